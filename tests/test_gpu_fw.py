@@ -1,0 +1,156 @@
+"""GPU parity of the Frank-Wolfe loop against the CPU oracle (port of the reference).
+
+Tolerances (from the spec contract):
+  FP64 mode       link flows within 1e-6 relative, relative gap and VHT within 1e-6
+  FP32-path mode  link flows within 1e-4 relative (of the largest flow)
+  shortest paths  labels bit-exact in FP64 (integer and continuous weights)
+"""
+
+import numpy as np
+import pytest
+
+import oracle
+from traffic_assignment_gb300 import Solver, synth
+
+pytestmark = pytest.mark.gpu
+
+RTOL64 = 1e-6
+RTOL32 = 1e-4
+
+
+def _rel(a, b):
+    return np.abs(a - b).max() / max(1.0, np.abs(b).max())
+
+
+@pytest.fixture(scope="module")
+def small24():
+    return synth.make_small24()
+
+
+@pytest.fixture(scope="module")
+def grid416():
+    return synth.make_grid416()
+
+
+def test_aon_matches_oracle(built_lib, grid416):
+    net, dem = grid416
+    with Solver(net, dem, precision="fp64") as s:
+        for t in (net.fft, net.fft * 1.7 + 0.3):
+            y = s.aon(t)
+            ref = oracle.aon(net, dem, t)
+            assert _rel(y, ref) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["small24", "grid416"])
+def test_fw_fp64_parity(built_lib, name):
+    net, dem = synth.make_workload(name)
+    iters = 60
+    ref = oracle.frankwolfe(net, dem, threads=1, max_iters=iters)
+    with Solver(net, dem, precision="fp64") as s:
+        r = s.solve(max_iters=iters)
+        x, t = s.flows()
+        tr = s.trace()
+    assert r["iterations"] == iters and r["error_bits"] == 0
+    assert _rel(x, ref["x"]) < RTOL64
+    assert _rel(t, ref["t"]) < RTOL64
+    assert abs(r["relgap"] - ref["relgap"]) <= RTOL64 * abs(ref["relgap"])
+    assert abs(r["total_cost"] - ref["total_cost"]) <= RTOL64 * abs(ref["total_cost"])
+    assert abs(r["objective"] - ref["objective"]) <= RTOL64 * abs(ref["objective"])
+    # per-iteration log: objective, relgap, average excess cost, VHT, lambda
+    np.testing.assert_allclose(tr[:, 0], ref["trace"][:, 0], rtol=RTOL64)
+    np.testing.assert_allclose(tr[:, 1], ref["trace"][:, 1], rtol=RTOL64)
+    np.testing.assert_allclose(tr[:, 3], ref["trace"][:, 3], rtol=RTOL64)
+    np.testing.assert_array_equal(tr[:, 4], ref["trace"][:, 4])
+
+
+@pytest.mark.parametrize("name", ["small24", "grid416"])
+def test_fw_fp32_paths(built_lib, name):
+    net, dem = synth.make_workload(name)
+    ref = oracle.frankwolfe(net, dem, threads=1, max_iters=40)
+    with Solver(net, dem, precision="fp32") as s:
+        r = s.solve(max_iters=40)
+        x, _ = s.flows()
+    assert r["error_bits"] == 0
+    assert _rel(x, ref["x"]) < RTOL32
+    assert abs(r["total_cost"] - ref["total_cost"]) <= RTOL32 * abs(ref["total_cost"])
+
+
+def test_relgap_stopping_rule(built_lib, grid416):
+    net, dem = grid416
+    ref = oracle.frankwolfe(net, dem, threads=1, target_relgap=1e-3)
+    with Solver(net, dem, precision="fp64") as s:
+        r = s.solve(target_relgap=1e-3)
+    assert r["iterations"] == ref["iterations"]
+    assert r["relgap"] <= 1e-3
+
+
+def test_sssp_labels_bit_exact(built_lib, grid416):
+    net, _ = grid416
+    va, ea = net.csr()
+    rng = np.random.default_rng(7)
+    w = net.fft * rng.uniform(0.5, 2.0, net.num_links)
+    srcs = np.arange(1, net.num_nodes + 1, 7)
+    dref, _ = oracle.sssp_all(va, ea, w, net.num_nodes + 1, srcs, net.first_thru_node)
+    with Solver(net, None) as s:
+        d, p = s.sssp(w, srcs)
+    np.testing.assert_array_equal(d, dref)
+    # every predecessor path re-sums to its label (cuda_sssp/sssp.cu:155-250)
+    for i, src in enumerate(srcs):
+        for v in range(1, net.num_nodes + 1):
+            if v == src:
+                assert p[i, v] == -1
+                continue
+            acc, u, steps = [], v, 0
+            while u != src:
+                k = p[i, u]
+                assert k >= 0 and net.term[k] == u
+                acc.append(w[k])
+                u = net.init[k]
+                steps += 1
+                assert steps <= net.num_nodes
+            tot = 0.0
+            for x in reversed(acc):
+                tot += x
+            assert tot == d[i, v]
+
+
+def test_sssp_integer_weights_bit_exact(built_lib):
+    net = synth.make_integer_graph(11, rows=9, cols=11, max_w=5)
+    va, ea = net.csr()
+    srcs = np.arange(1, net.num_nodes + 1)
+    dref, _ = oracle.sssp_all(va, ea, net.fft, net.num_nodes + 1, srcs, 1)
+    with Solver(net, None) as s:
+        d, _ = s.sssp(net.fft, srcs)
+    np.testing.assert_array_equal(d, dref)
+
+
+def test_first_thru_node_respected(built_lib):
+    net, dem = synth.make_grid416_centroids()
+    ref = oracle.frankwolfe(net, dem, threads=1, max_iters=25)
+    with Solver(net, dem, precision="fp64") as s:
+        r = s.solve(max_iters=25)
+        x, _ = s.flows()
+    assert _rel(x, ref["x"]) < RTOL64
+    assert abs(r["relgap"] - ref["relgap"]) <= RTOL64 * abs(ref["relgap"])
+
+
+def test_warm_start(built_lib, grid416):
+    net, dem = grid416
+    base = oracle.frankwolfe(net, dem, threads=1, max_iters=30)
+    ref = oracle.frankwolfe(net, dem, threads=1, max_iters=20, x0=base["x"])
+    with Solver(net, dem, precision="fp64") as s:
+        r = s.solve(max_iters=20, x0=base["x"])
+        x, _ = s.flows()
+    assert r["iterations"] == 20
+    assert _rel(x, ref["x"]) < RTOL64
+    assert abs(r["relgap"] - ref["relgap"]) <= RTOL64 * abs(ref["relgap"])
+
+
+def test_deterministic_fp32(built_lib, grid416):
+    net, dem = grid416
+    outs = []
+    for _ in range(2):
+        with Solver(net, dem, precision="fp32") as s:
+            s.solve(max_iters=15)
+            outs.append(s.flows()[0])
+    np.testing.assert_array_equal(outs[0], outs[1])

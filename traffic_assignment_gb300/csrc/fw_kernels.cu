@@ -1,0 +1,847 @@
+// fw_kernels.cu - sm_103a kernels of the Frank-Wolfe user-equilibrium loop.
+//
+//  k_sssp      all-origins shortest paths: one CTA per (scenario, origin) task,
+//              persistent over a work counter.  Labels live in shared memory and
+//              are corrected in bulk-synchronous rounds over a frontier bitmap;
+//              each warp compacts 32 bitmap words with a ballot-free prefix sum
+//              and relaxes the out-links of the set bits with shared-memory
+//              atomicMin on the label bits (non-negative IEEE values order as
+//              unsigned integers).  Replaces tap/sssp_pape.c:284-501 on the CPU
+//              and tap/pape_kernels.cu:122-204 on the GPU.
+//  k_aon       all-or-nothing loading (tap/tap_frankwolfe_pthread.c:262-310):
+//              recovers a deterministic predecessor tree from the labels, walks
+//              each OD pair's path accumulating demand per node in shared memory
+//              (64-bit fixed point, so the sums are exact and order-free), then
+//              scatters node totals onto the predecessor links.
+//  k_ls_pass   one pass of the 2^-k line search (tap/tap_functions.c:469-507)
+//              fused with the gap, Beckmann objective and VHT reductions
+//              (tap/tap_functions.c:83-152, 408-417): every candidate step of
+//              the pass is evaluated in the same sweep over the links.
+//  k_step      x += lambda*d, BPR cost and derivative update and the
+//              shortest-path weights for the next iteration
+//              (tap/tap_frankwolfe_pthread.c:737-739, tap/tap_functions.c:55-65).
+#include "fw_kernels.cuh"
+
+#include <cfloat>
+#include <cstdio>
+
+namespace tapgpu {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+template <typename T>
+struct DT;
+template <>
+struct DT<float> {
+  using U = unsigned int;
+  static constexpr U kInf = 0x7f800000u;
+  __device__ static __forceinline__ U bits(float v) { return __float_as_uint(v); }
+  __device__ static __forceinline__ float val(U b) { return __uint_as_float(b); }
+  __device__ static __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+};
+template <>
+struct DT<double> {
+  using U = unsigned long long;
+  static constexpr U kInf = 0x7ff0000000000000ull;
+  __device__ static __forceinline__ U bits(double v) {
+    return static_cast<U>(__double_as_longlong(v));
+  }
+  __device__ static __forceinline__ double val(U b) {
+    return __longlong_as_double(static_cast<long long>(b));
+  }
+  __device__ static __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+};
+
+template <typename U>
+__device__ __forceinline__ U vload(const U* p) {
+  return *reinterpret_cast<const volatile U*>(p);
+}
+
+__host__ __device__ __forceinline__ size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
+
+// position of the n-th (0-based) set bit of w; w must have more than n set bits
+__device__ __forceinline__ int nth_set_bit(unsigned w, int n) {
+  int pos = 0;
+  int c = __popc(w & 0xffffu);
+  if (n >= c) { n -= c; pos += 16; w >>= 16; }
+  c = __popc(w & 0xffu);
+  if (n >= c) { n -= c; pos += 8; w >>= 8; }
+  c = __popc(w & 0xfu);
+  if (n >= c) { n -= c; pos += 4; w >>= 4; }
+  c = __popc(w & 0x3u);
+  if (n >= c) { n -= c; pos += 2; w >>= 2; }
+  c = static_cast<int>(w & 1u);
+  if (n >= c) pos += 1;
+  return pos;
+}
+
+template <typename T>
+__device__ __forceinline__ const T* weights_of(const PathArgs& a, int scen);
+template <>
+__device__ __forceinline__ const float* weights_of<float>(const PathArgs& a, int scen) {
+  return a.w32 + static_cast<size_t>(scen) * a.g.m;
+}
+template <>
+__device__ __forceinline__ const double* weights_of<double>(const PathArgs& a, int scen) {
+  return a.w64 + static_cast<size_t>(scen) * a.g.m;
+}
+
+// Relax the out-links of v; returns 1 if any head label dropped.
+template <typename T>
+__device__ __forceinline__ int relax_node(int v, int src, const Graph& g, const T* __restrict__ wt,
+                                          typename DT<T>::U* dist, unsigned* nxt) {
+  using U = typename DT<T>::U;
+  if (v < g.first_thru && v != src) return 0;  // zones are never passed through
+  const T du = DT<T>::val(vload(dist + v));
+  const int e1 = __ldg(g.row_ptr + v + 1);
+  int pushed = 0;
+  for (int e = __ldg(g.row_ptr + v); e < e1; ++e) {
+    const int h = __ldg(g.head + e);
+    const U nb = DT<T>::bits(DT<T>::add(du, __ldg(wt + e)));
+    if (nb < vload(dist + h)) {
+      const U old = atomicMin(dist + h, nb);
+      if (nb < old) {
+        const unsigned bit = 1u << (h & 31);
+        if (!(vload(nxt + (h >> 5)) & bit)) atomicOr(nxt + (h >> 5), bit);
+        pushed = 1;
+      }
+    }
+  }
+  return pushed;
+}
+
+template <typename T, int BLOCK, bool SMEM>
+__global__ void __launch_bounds__(BLOCK) k_sssp(PathArgs a) {
+  using U = typename DT<T>::U;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int sh_task;
+  const int n1 = a.g.n1;
+  const int nwords = (n1 + 31) >> 5;
+  unsigned char* base =
+      SMEM ? smem_raw
+           : static_cast<unsigned char*>(a.scratch) + static_cast<size_t>(blockIdx.x) * a.scratch_stride;
+  U* dist = reinterpret_cast<U*>(base);
+  unsigned* bm0 = reinterpret_cast<unsigned*>(base + align16(sizeof(U) * n1));
+  unsigned* bm1 = bm0 + nwords;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  constexpr int kWarps = BLOCK / 32;
+
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) sh_task = atomicAdd(a.counter, 1) + a.task_begin;
+    __syncthreads();
+    const int task = sh_task;
+    if (task >= a.task_end) break;
+    const int slot = task / a.num_sources;
+    const int scen = a.scen_list ? a.scen_list[slot] : 0;
+    if (a.state && a.state[scen].done) continue;
+    const int src = a.sources[task - slot * a.num_sources];
+    const T* wt = weights_of<T>(a, scen);
+
+    for (int v = threadIdx.x; v < n1; v += BLOCK) dist[v] = DT<T>::kInf;
+    for (int i = threadIdx.x; i < 2 * nwords; i += BLOCK) bm0[i] = 0u;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      dist[src] = DT<T>::bits(T(0));
+      bm0[src >> 5] = 1u << (src & 31);
+    }
+    __syncthreads();
+
+    unsigned* cur = bm0;
+    unsigned* nxt = bm1;
+    int rounds = 0;
+    const int nchunks = (nwords + 31) >> 5;
+    for (;;) {
+      int pushed = 0;
+      for (int c = warp; c < nchunks; c += kWarps) {
+        const int wi = (c << 5) + lane;
+        unsigned word = 0u;
+        if (wi < nwords) {
+          word = cur[wi];
+          if (word) cur[wi] = 0u;
+        }
+        const int cnt = __popc(word);
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(kFull, incl, o);
+          if (lane >= o) incl += y;
+        }
+        const int total = __shfl_sync(kFull, incl, 31);
+        for (int b = 0; b < total; b += 32) {
+          const int j = b + lane;
+          int owner = 0;  // number of lanes whose inclusive count is <= j
+#pragma unroll
+          for (int step = 16; step >= 1; step >>= 1) {
+            const int probe = __shfl_sync(kFull, incl, owner + step - 1);
+            if (probe <= j) owner += step;
+          }
+          owner &= 31;
+          const unsigned ow = __shfl_sync(kFull, word, owner);
+          const int oincl = __shfl_sync(kFull, incl, owner);
+          if (j < total) {
+            const int rank = j - (oincl - __popc(ow));
+            const int v = (((c << 5) + owner) << 5) + nth_set_bit(ow, rank);
+            pushed |= relax_node<T>(v, src, a.g, wt, dist, nxt);
+          }
+        }
+      }
+      const int more = __syncthreads_or(pushed);
+      if (!more) break;
+      unsigned* tmp = cur;
+      cur = nxt;
+      nxt = tmp;
+      if (++rounds > a.max_rounds) {
+        if (threadIdx.x == 0) atomicOr(a.err, kErrRounds);
+        break;
+      }
+    }
+    T* out = static_cast<T*>(a.dist) + static_cast<size_t>(task - a.task_begin) * n1;
+    for (int v = threadIdx.x; v < n1; v += BLOCK) out[v] = DT<T>::val(dist[v]);
+  }
+}
+
+template <typename T, int BLOCK, bool SMEM>
+__global__ void __launch_bounds__(BLOCK) k_aon(PathArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int sh_task;
+  const int n1 = a.g.n1;
+  unsigned char* base =
+      SMEM ? smem_raw
+           : static_cast<unsigned char*>(a.scratch) + static_cast<size_t>(blockIdx.x) * a.scratch_stride;
+  T* dS = reinterpret_cast<T*>(base);                         // labels, then ...
+  long long* thr = reinterpret_cast<long long*>(base);        // ... node throughput
+  int* pred = reinterpret_cast<int*>(base + align16(sizeof(long long) * n1));
+  int* parent = pred + n1;
+  const int F = a.g.first_thru;
+
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) sh_task = atomicAdd(a.counter, 1) + a.task_begin;
+    __syncthreads();
+    const int task = sh_task;
+    if (task >= a.task_end) break;
+    const int slot = task / a.num_sources;
+    const int scen = a.scen_list ? a.scen_list[slot] : 0;
+    if (a.state && a.state[scen].done) continue;
+    const int sidx = task - slot * a.num_sources;
+    const int src = a.sources[sidx];
+    const T* wt = weights_of<T>(a, scen);
+    const T* din = static_cast<const T*>(a.dist) + static_cast<size_t>(task - a.task_begin) * n1;
+
+    for (int v = threadIdx.x; v < n1; v += BLOCK) dS[v] = din[v];
+    __syncthreads();
+
+    // Predecessor = lowest-numbered tight in-link from a strictly closer tail.
+    int pend = 0;
+    for (int v = threadIdx.x; v < n1; v += BLOCK) {
+      int p = -1;
+      const T dv = dS[v];
+      if (v != src && DT<T>::bits(dv) != DT<T>::kInf) {
+        p = -2;
+        const int i1 = __ldg(a.g.in_ptr + v + 1);
+        for (int i = __ldg(a.g.in_ptr + v); i < i1; ++i) {
+          const int k = __ldg(a.g.in_link + i);
+          const int u = __ldg(a.g.tail + k);
+          if (u < F && u != src) continue;
+          const T du = dS[u];
+          if (du < dv && DT<T>::add(du, __ldg(wt + k)) == dv) {
+            p = k;
+            break;
+          }
+        }
+        if (p == -2) pend = 1;
+      }
+      pred[v] = p;
+    }
+    pend = __syncthreads_or(pend);
+    // Rare: labels reached only over links too short to change them (zero or
+    // absorbed costs).  Attach such nodes level by level to already attached
+    // nodes of equal label, lowest link first, so the tree stays acyclic.
+    int guard = 0;
+    while (pend) {
+      for (int v = threadIdx.x; v < n1; v += BLOCK) {
+        if (pred[v] != -2) continue;
+        int c = -2;
+        const T dv = dS[v];
+        const int i1 = __ldg(a.g.in_ptr + v + 1);
+        for (int i = __ldg(a.g.in_ptr + v); i < i1; ++i) {
+          const int k = __ldg(a.g.in_link + i);
+          const int u = __ldg(a.g.tail + k);
+          if (u < F && u != src) continue;
+          if (!(u == src || pred[u] >= 0)) continue;
+          if (DT<T>::add(dS[u], __ldg(wt + k)) == dv) {
+            c = k;
+            break;
+          }
+        }
+        parent[v] = c;
+      }
+      __syncthreads();
+      int progress = 0, still = 0;
+      for (int v = threadIdx.x; v < n1; v += BLOCK) {
+        if (pred[v] != -2) continue;
+        if (parent[v] >= 0) {
+          pred[v] = parent[v];
+          progress = 1;
+        } else {
+          still = 1;
+        }
+      }
+      const int any_progress = __syncthreads_or(progress);
+      const int any_still = __syncthreads_or(still);
+      if (!any_still) break;
+      if (!any_progress || ++guard > n1) {
+        if (threadIdx.x == 0) atomicOr(a.err, kErrPending);
+        break;
+      }
+    }
+    for (int v = threadIdx.x; v < n1; v += BLOCK) {
+      const int p = pred[v];
+      parent[v] = p >= 0 ? __ldg(a.g.tail + p) : -1;
+    }
+    if (a.pred_out) {
+      int* po = a.pred_out + static_cast<size_t>(task - a.task_begin) * n1;
+      for (int v = threadIdx.x; v < n1; v += BLOCK) po[v] = pred[v] >= 0 ? pred[v] : -1;
+    }
+    __syncthreads();  // labels no longer needed: their space becomes the node totals
+    if (!a.do_load) continue;
+    for (int v = threadIdx.x; v < n1; v += BLOCK) thr[v] = 0;
+    __syncthreads();
+
+    const int j1 = __ldg(a.dem.od_ptr + sidx + 1);
+    for (int j = __ldg(a.dem.od_ptr + sidx) + threadIdx.x; j < j1; j += BLOCK) {
+      const int dest = __ldg(a.dem.od_dest + j);
+      if (dest == src || !(__ldg(a.dem.od_dem + j) > 0.0)) continue;
+      const unsigned long long q = static_cast<unsigned long long>(__ldg(a.dem.od_q + j));
+      if (dest < 0 || dest >= n1 || parent[dest] < 0) {
+        atomicOr(a.err, kErrNoPath);
+        a.err_info[0] = src;
+        a.err_info[1] = dest;
+        continue;
+      }
+      int v = dest;
+      int steps = 0;
+      while (v != src) {
+        if (v < 0 || ++steps > n1) {
+          atomicOr(a.err, kErrWalk);
+          break;
+        }
+        atomicAdd(reinterpret_cast<unsigned long long*>(thr + v), q);
+        v = parent[v];
+      }
+    }
+    __syncthreads();
+    unsigned long long* y = a.y_fx + static_cast<size_t>(scen) * a.g.m;
+    for (int v = threadIdx.x; v < n1; v += BLOCK) {
+      const long long q = thr[v];
+      if (q != 0) atomicAdd(y + pred[v], static_cast<unsigned long long>(q));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// link kernels
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ double pow2neg(int e) {
+  // 2^-e for 0 <= e <= 1022 (exact)
+  return __longlong_as_double(static_cast<long long>(1023 - e) << 52);
+}
+
+__device__ __forceinline__ double int_pow(double r, int n) {
+  double acc = 1.0, b = r;
+  while (n) {
+    if (n & 1) acc = __dmul_rn(acc, b);
+    n >>= 1;
+    if (n) b = __dmul_rn(b, b);
+  }
+  return acc;
+}
+
+__device__ __forceinline__ double pow_p(double r, double beta, unsigned char ip) {
+  return ip != 255 ? int_pow(r, ip) : pow(r, beta);
+}
+
+// tap/tap_functions.c:55-65
+__device__ __forceinline__ double bpr(double fft, double alpha, double beta, unsigned char ip,
+                                      double cap, double q) {
+  const double p = pow_p(__ddiv_rn(q, cap), beta, ip);
+  return __dmul_rn(fft, __dadd_rn(1.0, __dmul_rn(alpha, p)));
+}
+
+// d t / d q of the BPR cost
+__device__ __forceinline__ double bpr_dq(double fft, double alpha, double beta, unsigned char ip,
+                                         double cap, double q) {
+  if (beta == 0.0) return 0.0;
+  const double r = q / cap;
+  const double p1 = ip != 255 ? (ip >= 1 ? int_pow(r, ip - 1) : 0.0) : pow(r, beta - 1.0);
+  return fft * alpha * beta * p1 / cap;
+}
+
+// tap/tap_functions.c:112-126
+__device__ __forceinline__ double integral(double fft, double alpha, double beta, unsigned char ip,
+                                           double cap, double q) {
+  if (!(beta >= 0)) return 0.0;
+  const double a = __ddiv_rn(__ddiv_rn(alpha, pow_p(cap, beta, ip)), __dadd_rn(beta, 1.0));
+  return __dmul_rn(__dmul_rn(q, fft), __dadd_rn(1.0, __dmul_rn(a, pow_p(q, beta, ip))));
+}
+
+template <int N, int BLOCK>
+__device__ __forceinline__ void block_sum(double (&v)[N], double* sh /* [N][BLOCK/32] */) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int W = BLOCK / 32;
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    double s = v[i];
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) s = __dadd_rn(s, __shfl_down_sync(kFull, s, o));
+    if (lane == 0) sh[i * W + warp] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      double s = lane < W ? sh[i * W + lane] : 0.0;
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) s = __dadd_rn(s, __shfl_down_sync(kFull, s, o));
+      if (lane == 0) v[i] = s;
+    }
+  }
+}
+
+__device__ __forceinline__ int scen_of(const LinkArgs& a) {
+  return a.scen_list ? a.scen_list[blockIdx.y] : static_cast<int>(blockIdx.y);
+}
+
+// Last block of a scenario to arrive?  Every block must call this after
+// publishing its partials.
+__device__ __forceinline__ bool last_block(unsigned* arrive) {
+  __shared__ unsigned sh_ticket;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) sh_ticket = atomicAdd(arrive, 1u);
+  __syncthreads();
+  return sh_ticket == gridDim.x - 1;
+}
+
+__device__ __forceinline__ void write_weights(const LinkArgs& a, size_t i, double t) {
+  if (a.w32) a.w32[i] = __double2float_rn(t);
+  if (a.w64) a.w64[i] = t;
+}
+
+constexpr int kLinkBlock = 256;
+
+// x = AON volumes (fixed point), t = BPR(x), weights = t; resets the state.
+// With from_x set, x is taken as given (warm start).
+__global__ void __launch_bounds__(kLinkBlock) k_init_flows(LinkArgs a, int from_x) {
+  const int scen = scen_of(a);
+  const size_t off = static_cast<size_t>(scen) * a.m;
+  const double* cap = a.cap + off;
+  for (int k = blockIdx.x * kLinkBlock + threadIdx.x; k < a.m; k += gridDim.x * kLinkBlock) {
+    double x;
+    if (from_x) {
+      x = a.x[off + k];
+    } else {
+      x = static_cast<double>(static_cast<long long>(a.y_fx[off + k])) * a.inv_scale;
+      a.x[off + k] = x;
+    }
+    a.y_fx[off + k] = 0ull;
+    const double t = bpr(a.lp.fft[k], a.lp.alpha[k], a.lp.beta[k], a.lp.ipow[k], cap[k], x);
+    a.t[off + k] = t;
+    if (a.dtdx)
+      a.dtdx[off + k] = bpr_dq(a.lp.fft[k], a.lp.alpha[k], a.lp.beta[k], a.lp.ipow[k], cap[k], x);
+    write_weights(a, off + k, t);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ScenState& st = a.state[scen];
+    st.iter = 0;
+    st.ls_pending = 0;
+    st.ls_next = 1;
+    st.relgap = DBL_MAX;
+    st.best_lb = -DBL_MAX;
+    st.obj = 0.0;
+    st.gap = 0.0;
+    st.lambda = 0.0;
+    st.vht = 0.0;
+    st.avg_excess = 0.0;
+    st.g0 = 0.0;
+    st.vht_end = 0.0;
+    st.done = 0;
+  }
+}
+
+// weights = free-flow times (the first all-or-nothing of tap/tap_frankwolfe_pthread.c:672,706)
+__global__ void __launch_bounds__(kLinkBlock) k_set_free_flow(LinkArgs a) {
+  const int scen = scen_of(a);
+  const size_t off = static_cast<size_t>(scen) * a.m;
+  for (int k = blockIdx.x * kLinkBlock + threadIdx.x; k < a.m; k += gridDim.x * kLinkBlock) {
+    a.y_fx[off + k] = 0ull;
+    write_weights(a, off + k, a.lp.fft[k]);
+  }
+}
+
+__device__ void ls_decide(ScenState& st, const double* tot, int first_e, int pass, double total_demand) {
+  if (pass == 0) {
+    const double g0 = tot[0];
+    st.g0 = g0;
+    st.gap = -g0;
+    st.vht = tot[1];
+    st.obj = tot[2];
+    const double lb = st.obj - st.gap;
+    if (lb > st.best_lb) st.best_lb = lb;
+    if (st.best_lb != 0) st.relgap = (st.obj - st.best_lb) / fabs(st.best_lb);
+    st.avg_excess = -g0 / total_demand;
+    st.ls_pending = 1;
+    if (g0 >= 0) {
+      st.lambda = 0.0;
+      st.ls_pending = 0;
+      return;
+    }
+    if (tot[3] <= 0) {
+      st.lambda = 1.0;
+      st.ls_pending = 0;
+      return;
+    }
+  }
+  for (int j = 0; j < kLsPerPass; ++j) {
+    if (tot[4 + j] <= 0) {
+      st.lambda = pow2neg(first_e + j);
+      st.ls_pending = 0;
+      return;
+    }
+  }
+  st.ls_next = first_e + kLsPerPass;
+}
+
+// One line-search pass; pass 0 also forms d = y - x and the gap / objective /
+// VHT sums.  Candidates of this pass: 2^-(e0 .. e0+kLsPerPass-1).
+__global__ void __launch_bounds__(kLinkBlock) k_ls_pass(LinkArgs a) {
+  __shared__ double sh[kNumSums * (kLinkBlock / 32)];
+  const int scen = scen_of(a);
+  ScenState& st = a.state[scen];
+  if (st.done) return;
+  if (a.pass > 0 && !st.ls_pending) return;
+  const size_t off = static_cast<size_t>(scen) * a.m;
+  const int e0 = a.pass == 0 ? 1 : st.ls_next;
+  double acc[kNumSums];
+#pragma unroll
+  for (int i = 0; i < kNumSums; ++i) acc[i] = 0.0;
+  const double* cap = a.cap + off;
+  for (int k = blockIdx.x * kLinkBlock + threadIdx.x; k < a.m; k += gridDim.x * kLinkBlock) {
+    const double x = a.x[off + k];
+    const double fft = a.lp.fft[k], al = a.lp.alpha[k], be = a.lp.beta[k], c = cap[k];
+    const unsigned char ip = a.lp.ipow[k];
+    double d;
+    if (a.pass == 0) {
+      const double y = static_cast<double>(static_cast<long long>(a.y_fx[off + k])) * a.inv_scale;
+      a.y_fx[off + k] = 0ull;
+      d = __dsub_rn(y, x);
+      a.d[off + k] = d;
+      const double t = a.t[off + k];
+      acc[0] = __dadd_rn(acc[0], __dmul_rn(t, d));
+      acc[1] = __dadd_rn(acc[1], __dmul_rn(x, t));
+      acc[2] = __dadd_rn(acc[2], integral(fft, al, be, ip, c, x));
+      acc[3] = __dadd_rn(acc[3], __dmul_rn(bpr(fft, al, be, ip, c, __dadd_rn(x, d)), d));
+    } else {
+      d = a.d[off + k];
+    }
+#pragma unroll
+    for (int j = 0; j < kLsPerPass; ++j) {
+      const double lam = pow2neg(e0 + j);
+      const double q = __dadd_rn(x, __dmul_rn(lam, d));
+      acc[4 + j] = __dadd_rn(acc[4 + j], __dmul_rn(bpr(fft, al, be, ip, c, q), d));
+    }
+  }
+  block_sum<kNumSums, kLinkBlock>(acc, sh);
+  double* part = a.partials + (static_cast<size_t>(scen) * gridDim.x + blockIdx.x) * kNumSums;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int i = 0; i < kNumSums; ++i) part[i] = acc[i];
+  }
+  if (!last_block(a.arrive + scen)) return;
+  if (threadIdx.x == 0) {
+    double tot[kNumSums];
+    for (int i = 0; i < kNumSums; ++i) tot[i] = 0.0;
+    const double* p0 = a.partials + static_cast<size_t>(scen) * gridDim.x * kNumSums;
+    for (unsigned b = 0; b < gridDim.x; ++b)
+      for (int i = 0; i < kNumSums; ++i)
+        tot[i] = __dadd_rn(tot[i], vload(p0 + b * kNumSums + i));
+    ls_decide(st, tot, e0, a.pass, a.total_demand);
+    a.arrive[scen] = 0u;
+  }
+}
+
+// Continue the halving sequence one candidate at a time up to the reference's
+// cap of 1000 halvings (never reached on valid inputs).  Single block.
+__global__ void __launch_bounds__(1024) k_ls_fallback(LinkArgs a) {
+  __shared__ double sh[32];
+  __shared__ int sh_found;
+  const int scen = scen_of(a);
+  ScenState& st = a.state[scen];
+  if (st.done || !st.ls_pending) return;
+  const size_t off = static_cast<size_t>(scen) * a.m;
+  const double* cap = a.cap + off;
+  for (int e = st.ls_next; e <= kLsMaxHalvings; ++e) {
+    double s = 0.0;
+    const double lam = e <= 1022 ? pow2neg(e) : 0.0;
+    for (int k = threadIdx.x; k < a.m; k += blockDim.x) {
+      const double x = a.x[off + k], d = a.d[off + k];
+      const double q = __dadd_rn(x, __dmul_rn(lam, d));
+      s = __dadd_rn(s, __dmul_rn(bpr(a.lp.fft[k], a.lp.alpha[k], a.lp.beta[k], a.lp.ipow[k],
+                                     cap[k], q), d));
+    }
+    for (int o = 16; o >= 1; o >>= 1) s += __shfl_down_sync(kFull, s, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (unsigned w = 0; w < blockDim.x / 32; ++w) t += sh[w];
+      sh_found = t <= 0 ? 1 : 0;
+      if (sh_found) {
+        st.lambda = lam;
+        st.ls_pending = 0;
+      }
+    }
+    __syncthreads();
+    if (sh_found) return;
+  }
+  if (threadIdx.x == 0) {
+    st.lambda = 0.0;  // tap/tap_functions.c:506 returns lambda_left == 0
+    st.ls_pending = 0;
+    atomicOr(a.err, kErrLineSearch);
+  }
+}
+
+// x += lambda d; t = BPR(x); next weights; iteration bookkeeping.
+__global__ void __launch_bounds__(kLinkBlock) k_step(LinkArgs a) {
+  __shared__ double sh[1 * (kLinkBlock / 32)];
+  const int scen = scen_of(a);
+  ScenState& st = a.state[scen];
+  if (st.done) return;
+  const size_t off = static_cast<size_t>(scen) * a.m;
+  const double lam = st.lambda;
+  const int it = st.iter;
+  const bool tape = a.x_hist && it < a.hist_cap;
+  const size_t hoff = tape ? (static_cast<size_t>(scen) * a.hist_cap + it) * a.m : 0;
+  const double* cap = a.cap + off;
+  double acc[1] = {0.0};
+  for (int k = blockIdx.x * kLinkBlock + threadIdx.x; k < a.m; k += gridDim.x * kLinkBlock) {
+    const double x0 = a.x[off + k];
+    const double d = a.d[off + k];
+    if (tape) {
+      a.x_hist[hoff + k] = x0;
+      a.d_hist[hoff + k] = d;
+    }
+    const double x = __dadd_rn(x0, __dmul_rn(lam, d));
+    a.x[off + k] = x;
+    const double fft = a.lp.fft[k], al = a.lp.alpha[k], be = a.lp.beta[k], c = cap[k];
+    const unsigned char ip = a.lp.ipow[k];
+    const double t = bpr(fft, al, be, ip, c, x);
+    a.t[off + k] = t;
+    if (a.dtdx) a.dtdx[off + k] = bpr_dq(fft, al, be, ip, c, x);
+    write_weights(a, off + k, t);
+    acc[0] = __dadd_rn(acc[0], __dmul_rn(x, t));
+  }
+  block_sum<1, kLinkBlock>(acc, sh);
+  double* part = a.partials + (static_cast<size_t>(scen) * gridDim.x + blockIdx.x) * kNumSums;
+  if (threadIdx.x == 0) part[0] = acc[0];
+  if (!last_block(a.arrive + scen)) return;
+  if (threadIdx.x == 0) {
+    double v = 0.0;
+    const double* p0 = a.partials + static_cast<size_t>(scen) * gridDim.x * kNumSums;
+    for (unsigned b = 0; b < gridDim.x; ++b) v = __dadd_rn(v, vload(p0 + b * kNumSums));
+    st.vht_end = v;
+    if (tape) a.lam_hist[static_cast<size_t>(scen) * a.hist_cap + it] = lam;
+    if (a.trace && it < a.trace_cap) {
+      double* r = a.trace + (static_cast<size_t>(scen) * a.trace_cap + it) * kTraceCols;
+      r[0] = st.obj;
+      r[1] = st.relgap;
+      r[2] = st.avg_excess;
+      r[3] = st.vht;
+      r[4] = lam;
+      r[5] = st.gap;
+      r[6] = it + 1;
+      r[7] = st.g0;
+    }
+    st.iter = it + 1;
+    if ((st.max_iters > 0 && st.iter >= st.max_iters) ||
+        (st.target_relgap > 0 && !(st.relgap > st.target_relgap)))
+      st.done = 1;
+    a.arrive[scen] = 0u;
+  }
+}
+
+// Raise a kernel's dynamic shared-memory limit to the device maximum once, so
+// that launches inside a stream capture never change function attributes.
+template <typename Fn>
+cudaError_t allow_max_smem(Fn fn) {
+  static bool done = false;
+  if (done) return cudaSuccess;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, fn);
+  if (e != cudaSuccess) return e;
+  // the opt-in limit covers static and dynamic shared memory together
+  const int dyn = max_smem_optin(dev) - static_cast<int>(fa.sharedSizeBytes);
+  e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+  if (e == cudaSuccess)
+    done = true;
+  else
+    cudaGetLastError();
+  return e;
+}
+
+template <typename T, int BLOCK, bool SMEM>
+cudaError_t launch_sssp_t(const PathArgs& a, int grid, size_t smem, cudaStream_t s) {
+  auto fn = k_sssp<T, BLOCK, SMEM>;
+  if (SMEM) {
+    cudaError_t e = allow_max_smem(fn);
+    if (e != cudaSuccess) return e;
+  }
+  fn<<<grid, BLOCK, SMEM ? smem : 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <typename T, int BLOCK, bool SMEM>
+cudaError_t launch_aon_t(const PathArgs& a, int grid, size_t smem, cudaStream_t s) {
+  auto fn = k_aon<T, BLOCK, SMEM>;
+  if (SMEM) {
+    cudaError_t e = allow_max_smem(fn);
+    if (e != cudaSuccess) return e;
+  }
+  fn<<<grid, BLOCK, SMEM ? smem : 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t sssp_smem_bytes(int n1, bool fp64) {
+  const size_t words = (static_cast<size_t>(n1) + 31) / 32;
+  return align16((fp64 ? 8 : 4) * static_cast<size_t>(n1)) + 2 * 4 * words;
+}
+
+size_t aon_smem_bytes(int n1) {
+  return align16(8 * static_cast<size_t>(n1)) + 2 * 4 * static_cast<size_t>(n1);
+}
+
+int max_smem_optin(int device) {
+  int v = 0;
+  cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+  return v;
+}
+
+cudaError_t launch_sssp(const PathArgs& a, bool fp64, int grid, int block, bool smem,
+                        cudaStream_t s) {
+  const size_t bytes = sssp_smem_bytes(a.g.n1, fp64);
+#define TAPGPU_SSSP_CASE(B)                                                              \
+  if (block == B) {                                                                      \
+    if (fp64) return smem ? launch_sssp_t<double, B, true>(a, grid, bytes, s)            \
+                          : launch_sssp_t<double, B, false>(a, grid, bytes, s);          \
+    return smem ? launch_sssp_t<float, B, true>(a, grid, bytes, s)                       \
+                : launch_sssp_t<float, B, false>(a, grid, bytes, s);                     \
+  }
+  TAPGPU_SSSP_CASE(128)
+  TAPGPU_SSSP_CASE(256)
+  TAPGPU_SSSP_CASE(512)
+  TAPGPU_SSSP_CASE(1024)
+#undef TAPGPU_SSSP_CASE
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_aon(const PathArgs& a, bool fp64, int grid, int block, bool smem,
+                       cudaStream_t s) {
+  const size_t bytes = aon_smem_bytes(a.g.n1);
+#define TAPGPU_AON_CASE(B)                                                               \
+  if (block == B) {                                                                      \
+    if (fp64) return smem ? launch_aon_t<double, B, true>(a, grid, bytes, s)             \
+                          : launch_aon_t<double, B, false>(a, grid, bytes, s);           \
+    return smem ? launch_aon_t<float, B, true>(a, grid, bytes, s)                        \
+                : launch_aon_t<float, B, false>(a, grid, bytes, s);                      \
+  }
+  TAPGPU_AON_CASE(256)
+  TAPGPU_AON_CASE(512)
+  TAPGPU_AON_CASE(1024)
+#undef TAPGPU_AON_CASE
+  return cudaErrorInvalidValue;
+}
+
+template <typename T, int BLOCK, bool SMEM>
+int occ_sssp_t(size_t smem) {
+  auto fn = k_sssp<T, BLOCK, SMEM>;
+  if (SMEM && allow_max_smem(fn) != cudaSuccess) return 0;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, BLOCK, SMEM ? smem : 0) != cudaSuccess)
+    return 0;
+  return n;
+}
+
+template <typename T, int BLOCK, bool SMEM>
+int occ_aon_t(size_t smem) {
+  auto fn = k_aon<T, BLOCK, SMEM>;
+  if (SMEM && allow_max_smem(fn) != cudaSuccess) return 0;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, BLOCK, SMEM ? smem : 0) != cudaSuccess)
+    return 0;
+  return n;
+}
+
+int sssp_occupancy(bool fp64, int block, bool smem, int n1) {
+  const size_t bytes = sssp_smem_bytes(n1, fp64);
+#define TAPGPU_OCC(B)                                                                     \
+  if (block == B) {                                                                       \
+    if (fp64) return smem ? occ_sssp_t<double, B, true>(bytes) : occ_sssp_t<double, B, false>(bytes); \
+    return smem ? occ_sssp_t<float, B, true>(bytes) : occ_sssp_t<float, B, false>(bytes);   \
+  }
+  TAPGPU_OCC(128)
+  TAPGPU_OCC(256)
+  TAPGPU_OCC(512)
+  TAPGPU_OCC(1024)
+#undef TAPGPU_OCC
+  return 0;
+}
+
+int aon_occupancy(bool fp64, int block, bool smem, int n1) {
+  const size_t bytes = aon_smem_bytes(n1);
+#define TAPGPU_OCC(B)                                                                     \
+  if (block == B) {                                                                       \
+    if (fp64) return smem ? occ_aon_t<double, B, true>(bytes) : occ_aon_t<double, B, false>(bytes); \
+    return smem ? occ_aon_t<float, B, true>(bytes) : occ_aon_t<float, B, false>(bytes);     \
+  }
+  TAPGPU_OCC(256)
+  TAPGPU_OCC(512)
+  TAPGPU_OCC(1024)
+#undef TAPGPU_OCC
+  return 0;
+}
+
+cudaError_t launch_init_flows(const LinkArgs& a, int grid, cudaStream_t s) {
+  k_init_flows<<<dim3(grid, a.num_scen), kLinkBlock, 0, s>>>(a, a.pass);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_set_costs(const LinkArgs& a, int grid, cudaStream_t s) {
+  k_set_free_flow<<<dim3(grid, a.num_scen), kLinkBlock, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ls_pass(const LinkArgs& a, int grid, cudaStream_t s) {
+  k_ls_pass<<<dim3(grid, a.num_scen), kLinkBlock, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ls_fallback(const LinkArgs& a, cudaStream_t s) {
+  k_ls_fallback<<<dim3(1, a.num_scen), 1024, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_step(const LinkArgs& a, int grid, cudaStream_t s) {
+  k_step<<<dim3(grid, a.num_scen), kLinkBlock, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace tapgpu

@@ -1,0 +1,140 @@
+// fw_kernels.cuh - device data layout and kernel entry points of the GB300
+// Frank-Wolfe user-equilibrium solver.
+//
+// Layout in HBM (one network, S scenarios):
+//   forward star   row_ptr[n1+1], head[m]            (n1 = N+1 rows, row 0 unused)
+//   reverse star   in_ptr[n1+1], in_link[m]          (in-links of a node by link id)
+//   link table     tail[m], fft/alpha/beta[m] f64, ipow[m] u8 (integer BPR power)
+//   per scenario   cap[S][m], x[S][m], t[S][m], d[S][m] f64, y_fx[S][m] u64,
+//                  w32[S][m] f32 or w64[S][m] f64 (shortest-path weights)
+//   demand         CSR over source slots: od_ptr[Z+1], od_dest, od_q (fixed point)
+//   scratch        dist[chunk][n1] (f32 or f64) between the two path kernels
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace tapgpu {
+
+constexpr int kLsPerPass = 12;   // line-search candidates 2^-k evaluated per pass
+constexpr int kLsPasses = 5;     // passes captured per iteration (k up to 60)
+constexpr int kLsMaxHalvings = 1000;  // tap/tap_functions.c:472
+constexpr int kNumSums = 4 + kLsPerPass;  // g0, vht, obj, g(1), g(2^-j) ...
+constexpr int kTraceCols = 8;    // obj, relgap, avg_excess, vht, lambda, gap, iter, g0
+
+// error bits written to the device error word
+enum : int {
+  kErrRounds = 1,      // shortest-path rounds exceeded the node-count bound
+  kErrNoPath = 2,      // positive demand with an unreachable destination
+  kErrWalk = 4,        // predecessor walk longer than the node count
+  kErrPending = 8,     // predecessor tree could not be completed
+  kErrLineSearch = 16, // no step found within the halving cap
+};
+
+struct Graph {
+  int n1, m, first_thru;
+  const int* row_ptr;
+  const int* head;
+  const int* tail;
+  const int* in_ptr;
+  const int* in_link;
+};
+
+struct LinkParams {
+  const double* fft;
+  const double* alpha;
+  const double* beta;
+  const unsigned char* ipow;  // 0..15: integer power; 255: use pow()
+};
+
+struct ScenState {
+  int iter;        // FW iterations completed
+  int done;        // 1 once the stopping rule holds
+  int ls_pending;  // line search still searching
+  int ls_next;     // next halving exponent to test
+  int max_iters;   // <= 0: no cap
+  int pad0, pad1, pad2;
+  double target_relgap;
+  double relgap, best_lb, obj, gap, lambda, vht, avg_excess, g0;
+  double vht_end;  // VHT at the current x with the current costs
+};
+
+struct Demand {
+  const int* od_ptr;            // [num_sources+1]
+  const int* od_dest;           // destination node
+  const long long* od_q;        // demand in fixed point (2^-scale_bits units)
+  const double* od_dem;         // demand as given (for the no-path check)
+  double inv_scale;             // 2^-scale_bits
+  double total;                 // total demand (tap/tap_functions.c:377-386)
+};
+
+struct PathArgs {
+  Graph g;
+  const float* w32;             // [S][m] when fp32 paths
+  const double* w64;            // [S][m] when fp64 paths
+  const int* sources;           // source nodes
+  int num_sources;
+  const int* scen_list;         // scenario of each task block (nullptr: scenario 0)
+  const ScenState* state;       // skip tasks of finished scenarios (nullptr: never)
+  int task_begin, task_end;     // task t: scenario scen_list[t / num_sources],
+                                //         source sources[t % num_sources]
+  void* dist;                   // [(t - task_begin)][n1]
+  int* counter;                 // work counter, zero before launch
+  int* err;                     // error bits
+  int* err_info;                // [2]: origin, destination of a missing path
+  int max_rounds;
+  // all-or-nothing only
+  Demand dem;
+  unsigned long long* y_fx;     // [S][m]
+  int* pred_out;                // [(t - task_begin)][n1] predecessor links, optional
+  int do_load;                  // 0: predecessors only
+  void* scratch;                // per-CTA global scratch when the smem variant does not fit
+  long long scratch_stride;     // bytes per CTA
+};
+
+struct LinkArgs {
+  int m;
+  int num_scen;                 // scenarios in the launch (grid.y)
+  const int* scen_list;         // grid.y -> scenario id (nullptr: identity)
+  LinkParams lp;
+  const double* cap;            // [S][m]
+  double* x;                    // [S][m]
+  double* t;                    // [S][m]
+  double* d;                    // [S][m]
+  unsigned long long* y_fx;     // [S][m]
+  float* w32;                   // [S][m] or nullptr
+  double* w64;                  // [S][m] or nullptr
+  double* dtdx;                 // [S][m] or nullptr (derivative of the BPR cost)
+  double* partials;             // [S][gridDim.x][kNumSums]
+  unsigned int* arrive;         // [S] block arrival counters
+  ScenState* state;             // [S]
+  double* trace;                // [S][trace_cap][kTraceCols] or nullptr
+  int trace_cap;
+  double inv_scale;             // fixed point -> volume
+  double total_demand;
+  int pass;                     // line-search pass index
+  int* err;
+  double* x_hist;               // [S][hist_cap][m] flows before each step (adjoint tape)
+  double* d_hist;               // [S][hist_cap][m] directions
+  double* lam_hist;             // [S][hist_cap]
+  int hist_cap;
+};
+
+// launch helpers (implemented in fw_kernels.cu)
+size_t sssp_smem_bytes(int n1, bool fp64);
+size_t aon_smem_bytes(int n1);
+int max_smem_optin(int device);
+cudaError_t launch_sssp(const PathArgs& a, bool fp64, int grid, int block, bool smem,
+                        cudaStream_t s);
+cudaError_t launch_aon(const PathArgs& a, bool fp64, int grid, int block, bool smem,
+                       cudaStream_t s);
+// x = loaded volumes (a.pass == 0) or x as given (a.pass == 1); t = BPR(x); weights; state reset
+cudaError_t launch_init_flows(const LinkArgs& a, int grid, cudaStream_t s);
+// weights = free-flow times and y_fx = 0 (first all-or-nothing)
+cudaError_t launch_set_costs(const LinkArgs& a, int grid, cudaStream_t s);
+cudaError_t launch_ls_pass(const LinkArgs& a, int grid, cudaStream_t s);
+cudaError_t launch_ls_fallback(const LinkArgs& a, cudaStream_t s);
+cudaError_t launch_step(const LinkArgs& a, int grid, cudaStream_t s);
+int sssp_occupancy(bool fp64, int block, bool smem, int n1);  // resident CTAs per SM
+int aon_occupancy(bool fp64, int block, bool smem, int n1);
+
+}  // namespace tapgpu

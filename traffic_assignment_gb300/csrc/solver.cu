@@ -1,0 +1,1091 @@
+// solver.cu - host side of the GB300 Frank-Wolfe solver: builds the device
+// graph, demand and per-scenario state, enqueues FW iterations (captured into
+// CUDA graphs), and implements the tapgpu_* handle API of include/tap_gpu.h.
+#include "solver.cuh"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <numeric>
+
+namespace tapgpu {
+
+namespace {
+thread_local std::string g_message;
+}
+
+void set_message(const std::string& m) { g_message = m; }
+
+#define TG_CUDA(call)                                                                   \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess) {                                                            \
+      ::tapgpu::set_message(std::string(#call) + ": " + cudaGetErrorString(e_));       \
+      return TAPGPU_ERR_CUDA;                                                           \
+    }                                                                                   \
+  } while (0)
+
+#define TG_TRY(call)        \
+  do {                      \
+    int r_ = (call);        \
+    if (r_ != TAPGPU_OK) {  \
+      return r_;            \
+    }                       \
+  } while (0)
+
+Ctx::~Ctx() {
+  if (gexec) cudaGraphExecDestroy(gexec);
+  if (stream) cudaStreamDestroy(stream);
+  for (auto& m : owned) cudaFree(m.p);
+}
+
+int Ctx::alloc(void** p, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_message(std::string("cudaMalloc of ") + std::to_string(bytes) + " bytes: " +
+                cudaGetErrorString(e));
+    return TAPGPU_ERR_ALLOC;
+  }
+  owned.push_back({q, bytes});
+  *p = q;
+  return TAPGPU_OK;
+}
+
+static void free_owned(Ctx* c, void* p) {
+  if (!p) return;
+  for (size_t i = 0; i < c->owned.size(); ++i) {
+    if (c->owned[i].p == p) {
+      cudaFree(p);
+      c->owned.erase(c->owned.begin() + static_cast<long>(i));
+      return;
+    }
+  }
+}
+
+Graph Ctx::graph() const {
+  Graph g;
+  g.n1 = n1;
+  g.m = M;
+  g.first_thru = F;
+  g.row_ptr = row_ptr;
+  g.head = head;
+  g.tail = tail;
+  g.in_ptr = in_ptr;
+  g.in_link = in_link;
+  return g;
+}
+
+LinkParams Ctx::link_params() const {
+  LinkParams lp;
+  lp.fft = fft;
+  lp.alpha = alpha;
+  lp.beta = beta;
+  lp.ipow = ipow;
+  return lp;
+}
+
+Demand Ctx::demand() const {
+  Demand dm;
+  dm.od_ptr = od_ptr;
+  dm.od_dest = od_dest;
+  dm.od_q = od_q;
+  dm.od_dem = od_dem;
+  dm.inv_scale = inv_scale;
+  dm.total = total_demand;
+  return dm;
+}
+
+PathArgs Ctx::path_args(int nscen_slots) const {
+  PathArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.g = graph();
+  a.sources = sources;
+  a.num_sources = Z;
+  a.scen_list = scen_list;
+  a.state = state;
+  a.task_begin = 0;
+  a.task_end = nscen_slots * Z;
+  a.dist = dist;
+  a.counter = counters;
+  a.err = err;
+  a.err_info = err_info;
+  a.max_rounds = n1 + 2;
+  a.dem = demand();
+  a.y_fx = yfx;
+  a.do_load = 1;
+  a.scratch = path_scratch;
+  a.scratch_stride = 0;
+  return a;
+}
+
+LinkArgs Ctx::link_args(int nscen) const {
+  LinkArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.m = M;
+  a.num_scen = nscen;
+  a.scen_list = scen_list;
+  a.lp = link_params();
+  a.cap = cap;
+  a.x = x;
+  a.t = t;
+  a.d = d;
+  a.y_fx = yfx;
+  a.w32 = fp64 ? nullptr : w32;
+  a.w64 = fp64 ? w64 : nullptr;
+  a.dtdx = dtdx;
+  a.partials = partials;
+  a.arrive = arrive;
+  a.state = state;
+  a.trace = trace;
+  a.trace_cap = trace_cap;
+  a.inv_scale = inv_scale;
+  a.total_demand = total_demand;
+  a.err = err;
+  a.x_hist = x_hist;
+  a.d_hist = d_hist;
+  a.lam_hist = lam_hist;
+  a.hist_cap = hist_cap;
+  return a;
+}
+
+int Ctx::ensure_scenarios(int S) {
+  if (S <= S_cap) return TAPGPU_OK;
+  // release the old per-scenario arrays
+  void* olds[] = {cap, x, t, d, dtdx, yfx, w32, w64, state, partials, arrive, trace, scen_list,
+                  x_hist, d_hist, lam_hist};
+  for (void* p : olds) free_owned(this, p);
+  cap = x = t = d = dtdx = nullptr;
+  yfx = nullptr;
+  w32 = nullptr;
+  w64 = nullptr;
+  state = nullptr;
+  partials = nullptr;
+  arrive = nullptr;
+  trace = nullptr;
+  scen_list = nullptr;
+  x_hist = d_hist = lam_hist = nullptr;
+  const size_t sm = static_cast<size_t>(S) * M;
+  TG_TRY(alloc_n(&cap, sm));
+  TG_TRY(alloc_n(&x, sm));
+  TG_TRY(alloc_n(&t, sm));
+  TG_TRY(alloc_n(&d, sm));
+  TG_TRY(alloc_n(&yfx, sm));
+  if (fp64)
+    TG_TRY(alloc_n(&w64, sm));
+  else
+    TG_TRY(alloc_n(&w32, sm));
+  if (opt.record_tape) TG_TRY(alloc_n(&dtdx, sm));
+  TG_TRY(alloc_n(&state, static_cast<size_t>(S)));
+  TG_TRY(alloc_n(&partials, static_cast<size_t>(S) * link_grid * kNumSums));
+  TG_TRY(alloc_n(&arrive, static_cast<size_t>(S)));
+  TG_CUDA(cudaMemset(arrive, 0, sizeof(unsigned) * S));
+  trace_cap = S == 1 ? 100000 : 4096;
+  TG_TRY(alloc_n(&trace, static_cast<size_t>(S) * trace_cap * kTraceCols));
+  TG_TRY(alloc_n(&scen_list, static_cast<size_t>(S)));
+  if (opt.record_tape && opt.tape_capacity > 0) {
+    hist_cap = opt.tape_capacity;
+    TG_TRY(alloc_n(&x_hist, sm * hist_cap));
+    TG_TRY(alloc_n(&d_hist, sm * hist_cap));
+    TG_TRY(alloc_n(&lam_hist, static_cast<size_t>(S) * hist_cap));
+  }
+  S_cap = S;
+  if (gexec) {
+    cudaGraphExecDestroy(gexec);
+    gexec = nullptr;
+  }
+  g_nscen = -1;
+  return TAPGPU_OK;
+}
+
+int Ctx::plan_launches() {
+  cudaDeviceProp prop;
+  TG_CUDA(cudaGetDeviceProperties(&prop, device));
+  num_sms = prop.multiProcessorCount;
+  const int optin = max_smem_optin(device);
+  sssp_block = opt.sssp_block > 0 ? opt.sssp_block : 256;
+  aon_block = opt.aon_block > 0 ? opt.aon_block : 512;
+  // leave room for the kernels' static shared memory (a few words)
+  const size_t room = optin > 1024 ? static_cast<size_t>(optin - 1024) : 0;
+  sssp_smem = sssp_smem_bytes(n1, fp64) <= room;
+  aon_smem = aon_smem_bytes(n1) <= room;
+  int so = sssp_occupancy(fp64, sssp_block, sssp_smem, n1);
+  int ao = aon_occupancy(fp64, aon_block, aon_smem, n1);
+  if (so <= 0 || ao <= 0) {
+    set_message("no resident CTA fits for the shortest-path kernels");
+    return TAPGPU_ERR_UNSUPPORTED;
+  }
+  sssp_grid = so * num_sms;
+  aon_grid = ao * num_sms;
+  size_t scratch = 0;
+  if (!sssp_smem) scratch = std::max(scratch, sssp_smem_bytes(n1, fp64) * sssp_grid);
+  if (!aon_smem) scratch = std::max(scratch, aon_smem_bytes(n1) * aon_grid);
+  if (scratch) {
+    TG_TRY(alloc(&path_scratch, scratch));
+    path_scratch_bytes = scratch;
+  }
+  link_grid = std::max(1, std::min((M + 255) / 256, 2 * num_sms));
+  return TAPGPU_OK;
+}
+
+int Ctx::enqueue_paths(int nscen, bool load, const float* w32p, const double* w64p,
+                       unsigned long long* ydst, bool use_state) {
+  const int64_t tasks = static_cast<int64_t>(nscen) * Z;
+  for (int64_t t0 = 0; t0 < tasks; t0 += dist_tasks) {
+    const int64_t t1 = std::min(tasks, t0 + dist_tasks);
+    PathArgs a = path_args(nscen);
+    a.w32 = w32p;
+    a.w64 = w64p;
+    a.y_fx = ydst;
+    a.do_load = load ? 1 : 0;
+    a.task_begin = static_cast<int>(t0);
+    a.task_end = static_cast<int>(t1);
+    if (!use_state) {
+      a.state = nullptr;
+      a.scen_list = nullptr;
+    }
+    const int ntask = static_cast<int>(t1 - t0);
+    a.scratch_stride = static_cast<long long>(sssp_smem_bytes(n1, fp64));
+    TG_CUDA(cudaMemsetAsync(counters, 0, 2 * sizeof(int), stream));
+    a.counter = counters;
+    TG_CUDA(launch_sssp(a, fp64, std::min(sssp_grid, ntask), sssp_block, sssp_smem, stream));
+    a.counter = counters + 1;
+    a.scratch_stride = static_cast<long long>(aon_smem_bytes(n1));
+    TG_CUDA(launch_aon(a, fp64, std::min(aon_grid, ntask), aon_block, aon_smem, stream));
+  }
+  return TAPGPU_OK;
+}
+
+int Ctx::enqueue_iteration(int nscen) {
+  TG_TRY(enqueue_paths(nscen, true, w32, w64, yfx, true));
+  LinkArgs la = link_args(nscen);
+  for (int p = 0; p < kLsPasses; ++p) {
+    la.pass = p;
+    TG_CUDA(launch_ls_pass(la, link_grid, stream));
+  }
+  TG_CUDA(launch_ls_fallback(la, stream));
+  TG_CUDA(launch_step(la, link_grid, stream));
+  return TAPGPU_OK;
+}
+
+// State reset, first all-or-nothing at free-flow costs (or warm flows), costs.
+int Ctx::enqueue_initial(int nscen, bool warm) {
+  LinkArgs la = link_args(nscen);
+  if (!warm) {
+    TG_CUDA(launch_set_costs(la, link_grid, stream));
+    TG_TRY(enqueue_paths(nscen, true, w32, w64, yfx, true));
+    la.pass = 0;
+  } else {
+    la.pass = 1;
+  }
+  TG_CUDA(launch_init_flows(la, link_grid, stream));
+  return TAPGPU_OK;
+}
+
+int Ctx::run_graph(int iters, int nscen) {
+  if (!opt.use_graphs) {
+    for (int i = 0; i < iters; ++i) TG_TRY(enqueue_iteration(nscen));
+    return TAPGPU_OK;
+  }
+  if (!gexec || g_iters != iters || g_nscen != nscen) {
+    if (gexec) {
+      cudaGraphExecDestroy(gexec);
+      gexec = nullptr;
+    }
+    cudaGraph_t graph = nullptr;
+    TG_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    int rc = TAPGPU_OK;
+    for (int i = 0; i < iters && rc == TAPGPU_OK; ++i) rc = enqueue_iteration(nscen);
+    cudaError_t ec = cudaStreamEndCapture(stream, &graph);
+    if (rc != TAPGPU_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (ec != cudaSuccess) {
+      set_message(std::string("graph capture: ") + cudaGetErrorString(ec));
+      return TAPGPU_ERR_CUDA;
+    }
+    cudaError_t ei = cudaGraphInstantiate(&gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {
+      set_message(std::string("graph instantiate: ") + cudaGetErrorString(ei));
+      gexec = nullptr;
+      return TAPGPU_ERR_CUDA;
+    }
+    g_iters = iters;
+    g_nscen = nscen;
+  }
+  TG_CUDA(cudaGraphLaunch(gexec, stream));
+  return TAPGPU_OK;
+}
+
+int Ctx::sync_check() {
+  TG_CUDA(cudaStreamSynchronize(stream));
+  int e = 0;
+  TG_CUDA(cudaMemcpy(&e, err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e & kErrNoPath) {
+    int info[2] = {0, 0};
+    cudaMemcpy(info, err_info, sizeof(info), cudaMemcpyDeviceToHost);
+    set_message("ERROR: no path from " + std::to_string(info[0]) + " to " +
+                std::to_string(info[1]));
+    return TAPGPU_ERR_NO_PATH;
+  }
+  if (e & (kErrRounds | kErrWalk | kErrPending)) {
+    set_message("device loop hit its bound (error bits " + std::to_string(e) + ")");
+    return TAPGPU_ERR_NO_CONVERGENCE;
+  }
+  return TAPGPU_OK;
+}
+
+int Ctx::read_states(int S, std::vector<ScenState>& out) {
+  out.resize(S);
+  TG_CUDA(cudaMemcpyAsync(out.data(), state, sizeof(ScenState) * S, cudaMemcpyDeviceToHost,
+                          stream));
+  TG_CUDA(cudaStreamSynchronize(stream));
+  return TAPGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// construction
+// ---------------------------------------------------------------------------
+
+static int validate(const tapgpu_network* net, const tapgpu_demand* dem) {
+  if (!net || !net->init || !net->term || !net->capacity || !net->fft || !net->alpha ||
+      !net->beta) {
+    set_message("network arrays missing");
+    return TAPGPU_ERR_ARG;
+  }
+  if (net->num_nodes < 1 || net->num_links < 1 || net->num_nodes > (1 << 30) ||
+      net->num_links > (1ll << 31) - 2) {
+    set_message("network size out of range");
+    return TAPGPU_ERR_ARG;
+  }
+  if (net->num_zones < 0 || net->num_zones > net->num_nodes || net->first_thru_node < 0) {
+    set_message("zone count or first thru node out of range");
+    return TAPGPU_ERR_ARG;
+  }
+  for (int64_t k = 0; k < net->num_links; ++k) {
+    const int64_t a = net->init[k], b = net->term[k];
+    if (a < 1 || a > net->num_nodes || b < 1 || b > net->num_nodes) {
+      set_message("link " + std::to_string(k) + " has a node outside 1..N");
+      return TAPGPU_ERR_ARG;
+    }
+    if (!(net->fft[k] >= 0) || !std::isfinite(net->fft[k]) || !(net->alpha[k] >= 0) ||
+        !std::isfinite(net->alpha[k]) || !std::isfinite(net->beta[k]) ||
+        std::isnan(net->capacity[k])) {
+      set_message("link " + std::to_string(k) + " has an invalid cost parameter");
+      return TAPGPU_ERR_ARG;
+    }
+  }
+  if (dem) {
+    if (dem->num_origins < 0 || dem->num_origins > net->num_nodes ||
+        (dem->num_origins > 0 && (!dem->od_ptr || !dem->od_dest || !dem->od_demand))) {
+      set_message("demand arrays missing or origin count out of range");
+      return TAPGPU_ERR_ARG;
+    }
+    for (int64_t o = 1; o <= dem->num_origins; ++o)
+      if (dem->od_ptr[o + 1] < dem->od_ptr[o]) {
+        set_message("demand pointers not monotone");
+        return TAPGPU_ERR_ARG;
+      }
+    const int64_t nnz = dem->num_origins > 0 ? dem->od_ptr[dem->num_origins + 1] : 0;
+    for (int64_t i = 0; i < nnz; ++i)
+      if (dem->od_dest[i] < 0 || dem->od_dest[i] > net->num_nodes ||
+          std::isnan(dem->od_demand[i])) {
+        set_message("demand entry " + std::to_string(i) + " invalid");
+        return TAPGPU_ERR_ARG;
+      }
+  }
+  return TAPGPU_OK;
+}
+
+static int create_impl(const tapgpu_network* net, const tapgpu_demand* dem,
+                       const tapgpu_options* opt_in, Ctx** out) {
+  TG_TRY(validate(net, dem));
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    set_message("no CUDA device");
+    return TAPGPU_ERR_NO_DEVICE;
+  }
+  tapgpu_options opt;
+  tapgpu_default_options(&opt);
+  if (opt_in) opt = *opt_in;
+  if (opt.device < 0 || opt.device >= ndev) {
+    set_message("device ordinal out of range");
+    return TAPGPU_ERR_ARG;
+  }
+  TG_CUDA(cudaSetDevice(opt.device));
+  Ctx* c = new Ctx();
+  std::unique_ptr<Ctx> guard(c);
+  c->opt = opt;
+  c->device = opt.device;
+  c->fp64 = opt.precision == TAPGPU_FP64;
+  c->N = static_cast<int>(net->num_nodes);
+  c->n1 = c->N + 1;
+  c->M = static_cast<int>(net->num_links);
+  c->Z = static_cast<int>(dem ? dem->num_origins : net->num_zones);
+  c->F = static_cast<int>(std::min<int64_t>(net->first_thru_node, c->n1 + 1));
+  const int M = c->M, n1 = c->n1;
+
+  // links sorted by (init, term) as tap/parsetapfiles.c:528-540 orders them
+  c->perm.resize(M);
+  std::iota(c->perm.begin(), c->perm.end(), 0);
+  std::stable_sort(c->perm.begin(), c->perm.end(), [&](int64_t a, int64_t b) {
+    if (net->init[a] != net->init[b]) return net->init[a] < net->init[b];
+    return net->term[a] < net->term[b];
+  });
+  c->h_tail.resize(M);
+  c->h_head.resize(M);
+  c->h_cap.resize(M);
+  c->h_fft.resize(M);
+  c->h_alpha.resize(M);
+  c->h_beta.resize(M);
+  std::vector<unsigned char> ip(M);
+  double min_cap = DBL_MAX;
+  for (int k = 0; k < M; ++k) {
+    const int64_t e = c->perm[k];
+    c->h_tail[k] = static_cast<int>(net->init[e]);
+    c->h_head[k] = static_cast<int>(net->term[e]);
+    c->h_cap[k] = net->capacity[e];
+    c->h_fft[k] = net->fft[e];
+    c->h_alpha[k] = net->alpha[e];
+    c->h_beta[k] = net->beta[e];
+    const double b = net->beta[e];
+    ip[k] = (b >= 0 && b <= 15 && std::floor(b) == b) ? static_cast<unsigned char>(b) : 255;
+    if (c->h_cap[k] > 0.0 && c->h_cap[k] < min_cap) min_cap = c->h_cap[k];
+  }
+  // tap/tap_frankwolfe_pthread.c:654-669 zero capacity -> smallest nonzero capacity
+  for (int k = 0; k < M; ++k)
+    if (!(c->h_cap[k] > 0.0)) c->h_cap[k] = min_cap;
+
+  std::vector<int> rp(n1 + 1, 0), ip_in(n1 + 1, 0), inl(M);
+  for (int k = 0; k < M; ++k) {
+    rp[c->h_tail[k] + 1]++;
+    ip_in[c->h_head[k] + 1]++;
+  }
+  for (int v = 0; v < n1; ++v) {
+    rp[v + 1] += rp[v];
+    ip_in[v + 1] += ip_in[v];
+  }
+  {
+    std::vector<int> fill(ip_in.begin(), ip_in.end() - 1);
+    for (int k = 0; k < M; ++k) inl[fill[c->h_head[k]]++] = k;
+  }
+
+  TG_TRY(c->alloc_n(&c->row_ptr, n1 + 1));
+  TG_TRY(c->alloc_n(&c->head, M));
+  TG_TRY(c->alloc_n(&c->tail, M));
+  TG_TRY(c->alloc_n(&c->in_ptr, n1 + 1));
+  TG_TRY(c->alloc_n(&c->in_link, M));
+  TG_TRY(c->alloc_n(&c->fft, M));
+  TG_TRY(c->alloc_n(&c->alpha, M));
+  TG_TRY(c->alloc_n(&c->beta, M));
+  TG_TRY(c->alloc_n(&c->ipow, M));
+  TG_CUDA(cudaMemcpy(c->row_ptr, rp.data(), sizeof(int) * (n1 + 1), cudaMemcpyHostToDevice));
+  TG_CUDA(cudaMemcpy(c->head, c->h_head.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
+  TG_CUDA(cudaMemcpy(c->tail, c->h_tail.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
+  TG_CUDA(cudaMemcpy(c->in_ptr, ip_in.data(), sizeof(int) * (n1 + 1), cudaMemcpyHostToDevice));
+  TG_CUDA(cudaMemcpy(c->in_link, inl.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
+  TG_CUDA(cudaMemcpy(c->fft, c->h_fft.data(), sizeof(double) * M, cudaMemcpyHostToDevice));
+  TG_CUDA(cudaMemcpy(c->alpha, c->h_alpha.data(), sizeof(double) * M, cudaMemcpyHostToDevice));
+  TG_CUDA(cudaMemcpy(c->beta, c->h_beta.data(), sizeof(double) * M, cudaMemcpyHostToDevice));
+  TG_CUDA(cudaMemcpy(c->ipow, ip.data(), M, cudaMemcpyHostToDevice));
+
+  // demand as a CSR over origin slots 0..Z-1 (origin node = slot + 1)
+  const int Z = c->Z;
+  std::vector<int> optr(Z + 1, 0), odest;
+  std::vector<long long> oq;
+  std::vector<double> odem;
+  double total = 0.0, pos = 0.0;
+  if (dem && Z > 0) {
+    for (int o = 1; o <= Z; ++o)
+      for (int64_t i = dem->od_ptr[o]; i < dem->od_ptr[o + 1]; ++i) {
+        total += dem->od_demand[i];  // tap/tap_functions.c:377-386 sums every entry
+        if (dem->od_demand[i] > 0) pos += dem->od_demand[i];
+      }
+    // fixed point with headroom: every node/link total stays below 2^61
+    int bits = 40;
+    if (pos > 1.0) bits = std::min(40, 61 - static_cast<int>(std::ceil(std::log2(pos))) - 1);
+    c->scale_bits = bits;
+    const double scale = std::ldexp(1.0, bits);
+    for (int o = 1; o <= Z; ++o) {
+      for (int64_t i = dem->od_ptr[o]; i < dem->od_ptr[o + 1]; ++i) {
+        const double v = dem->od_demand[i];
+        odest.push_back(static_cast<int>(dem->od_dest[i]));
+        odem.push_back(v);
+        oq.push_back(v > 0 ? std::llrint(v * scale) : 0);
+      }
+      optr[o] = static_cast<int>(odest.size());
+    }
+  }
+  c->inv_scale = std::ldexp(1.0, -c->scale_bits);
+  c->total_demand = total;
+  std::vector<int> src(std::max(Z, 1));
+  for (int i = 0; i < Z; ++i) src[i] = i + 1;
+  TG_TRY(c->alloc_n(&c->od_ptr, Z + 1));
+  TG_TRY(c->alloc_n(&c->od_dest, std::max<size_t>(odest.size(), 1)));
+  TG_TRY(c->alloc_n(&c->od_q, std::max<size_t>(oq.size(), 1)));
+  TG_TRY(c->alloc_n(&c->od_dem, std::max<size_t>(odem.size(), 1)));
+  TG_TRY(c->alloc_n(&c->sources, std::max(Z, 1)));
+  TG_CUDA(cudaMemcpy(c->od_ptr, optr.data(), sizeof(int) * (Z + 1), cudaMemcpyHostToDevice));
+  if (!odest.empty()) {
+    TG_CUDA(cudaMemcpy(c->od_dest, odest.data(), sizeof(int) * odest.size(),
+                       cudaMemcpyHostToDevice));
+    TG_CUDA(cudaMemcpy(c->od_q, oq.data(), sizeof(long long) * oq.size(), cudaMemcpyHostToDevice));
+    TG_CUDA(cudaMemcpy(c->od_dem, odem.data(), sizeof(double) * odem.size(),
+                       cudaMemcpyHostToDevice));
+  }
+  TG_CUDA(cudaMemcpy(c->sources, src.data(), sizeof(int) * src.size(), cudaMemcpyHostToDevice));
+
+  TG_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  TG_TRY(c->plan_launches());
+  TG_TRY(c->alloc_n(&c->counters, 2));
+  TG_TRY(c->alloc_n(&c->err, 1));
+  TG_TRY(c->alloc_n(&c->err_info, 2));
+  TG_CUDA(cudaMemset(c->err, 0, sizeof(int)));
+
+  // shortest-path label scratch between the two path kernels
+  const size_t tb = static_cast<size_t>(n1) * (c->fp64 ? 8 : 4);
+  int64_t chunk = opt.chunk_tasks > 0 ? opt.chunk_tasks
+                                      : std::max<int64_t>(1, (int64_t(2) << 30) / static_cast<int64_t>(tb));
+  chunk = std::max<int64_t>(1, std::min<int64_t>(chunk, 1 << 30));
+  c->dist_tasks = std::min<int64_t>(chunk, std::max<int64_t>(Z, 1) * 4096);
+  TG_TRY(c->alloc(&c->dist, tb * c->dist_tasks));
+  TG_TRY(c->alloc_n(&c->api_w32, M));
+  TG_TRY(c->alloc_n(&c->api_w64, M));
+  TG_TRY(c->alloc_n(&c->api_yfx, M));
+  TG_TRY(c->ensure_scenarios(1));
+  std::vector<double> capv(c->h_cap);
+  TG_CUDA(cudaMemcpy(c->cap, capv.data(), sizeof(double) * M, cudaMemcpyHostToDevice));
+  *out = guard.release();
+  return TAPGPU_OK;
+}
+
+static int upload_states(Ctx* c, int S, int max_iters, double target) {
+  std::vector<ScenState> st(S);
+  for (auto& s : st) {
+    std::memset(&s, 0, sizeof(s));
+    s.max_iters = max_iters;
+    s.target_relgap = target;
+    s.relgap = DBL_MAX;
+    s.best_lb = -DBL_MAX;
+  }
+  TG_CUDA(cudaMemcpyAsync(c->state, st.data(), sizeof(ScenState) * S, cudaMemcpyHostToDevice,
+                          c->stream));
+  TG_CUDA(cudaMemsetAsync(c->err, 0, sizeof(int), c->stream));
+  return TAPGPU_OK;
+}
+
+static int iterate_until_done(Ctx* c, int S, int max_iters, std::vector<ScenState>& st) {
+  // iterations per graph launch: enough to hide launch gaps, few enough that
+  // finished scenarios do not linger
+  int per = c->opt.iters_per_launch > 0 ? c->opt.iters_per_launch : (S == 1 ? 8 : 4);
+  std::vector<int> active;
+  for (;;) {
+    TG_TRY(c->read_states(S, st));
+    active.clear();
+    for (int s = 0; s < S; ++s)
+      if (!st[s].done) active.push_back(s);
+    TG_TRY(c->sync_check());
+    if (active.empty()) break;
+    int n = per;
+    if (max_iters > 0) {
+      int left = 0;
+      for (int s : active) left = std::max(left, max_iters - st[s].iter);
+      n = std::max(1, std::min(n, left));
+    }
+    if (active != c->h_scen_list) {
+      TG_CUDA(cudaMemcpyAsync(c->scen_list, active.data(), sizeof(int) * active.size(),
+                              cudaMemcpyHostToDevice, c->stream));
+      c->h_scen_list = active;
+    }
+    TG_TRY(c->run_graph(n, static_cast<int>(active.size())));
+  }
+  return TAPGPU_OK;
+}
+
+static void fill_result(const ScenState& s, int err_bits, tapgpu_result* r) {
+  r->iterations = s.iter;
+  r->error_bits = err_bits;
+  r->objective = s.obj;
+  r->relgap = s.relgap;
+  r->total_cost = s.vht_end;
+  r->avg_excess = s.avg_excess;
+  r->lambda_last = s.lambda;
+}
+
+}  // namespace tapgpu
+
+using tapgpu::Ctx;
+
+struct tapgpu_ctx {
+  Ctx* c;
+};
+
+extern "C" {
+
+void tapgpu_default_options(tapgpu_options* o) {
+  std::memset(o, 0, sizeof(*o));
+  o->precision = TAPGPU_FP64;
+  o->device = 0;
+  o->use_graphs = 1;
+}
+
+const char* tapgpu_status_string(int s) {
+  switch (s) {
+    case TAPGPU_OK: return "ok";
+    case TAPGPU_ERR_ARG: return "invalid argument";
+    case TAPGPU_ERR_CUDA: return "CUDA error";
+    case TAPGPU_ERR_NO_PATH: return "no path for a positive demand";
+    case TAPGPU_ERR_NO_CONVERGENCE: return "device loop hit its bound";
+    case TAPGPU_ERR_ALLOC: return "allocation failed";
+    case TAPGPU_ERR_UNSUPPORTED: return "unsupported size";
+    case TAPGPU_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+  }
+}
+
+const char* tapgpu_last_message(void) { return tapgpu::g_message.c_str(); }
+
+int tapgpu_create(const tapgpu_network* net, const tapgpu_demand* dem, const tapgpu_options* opt,
+                  tapgpu_ctx** out) {
+  if (!out) return TAPGPU_ERR_ARG;
+  *out = nullptr;
+  Ctx* c = nullptr;
+  int rc = tapgpu::create_impl(net, dem, opt, &c);
+  if (rc != TAPGPU_OK) return rc;
+  *out = new tapgpu_ctx{c};
+  return TAPGPU_OK;
+}
+
+void tapgpu_destroy(tapgpu_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->c->device);
+  delete ctx->c;
+  delete ctx;
+}
+
+int tapgpu_set_capacity(tapgpu_ctx* ctx, const double* capacity) {
+  if (!ctx || !capacity) return TAPGPU_ERR_ARG;
+  Ctx* c = ctx->c;
+  double min_cap = DBL_MAX;
+  for (int k = 0; k < c->M; ++k) {
+    const double v = capacity[c->perm[k]];
+    if (v > 0 && v < min_cap) min_cap = v;
+  }
+  for (int k = 0; k < c->M; ++k) {
+    const double v = capacity[c->perm[k]];
+    c->h_cap[k] = v > 0 ? v : min_cap;
+  }
+  TG_CUDA(cudaSetDevice(c->device));
+  TG_CUDA(cudaMemcpy(c->cap, c->h_cap.data(), sizeof(double) * c->M, cudaMemcpyHostToDevice));
+  return TAPGPU_OK;
+}
+
+int tapgpu_solve_begin(tapgpu_ctx* ctx, int max_iters, double target_relgap, const double* x0) {
+  if (!ctx || (max_iters <= 0 && !(target_relgap > 0))) {
+    tapgpu::set_message("need an iteration cap or a positive relative-gap target");
+    return TAPGPU_ERR_ARG;
+  }
+  Ctx* c = ctx->c;
+  TG_CUDA(cudaSetDevice(c->device));
+  TG_TRY(c->ensure_scenarios(1));
+  TG_CUDA(cudaMemcpy(c->cap, c->h_cap.data(), sizeof(double) * c->M, cudaMemcpyHostToDevice));
+  std::vector<int> one{0};
+  TG_CUDA(cudaMemcpyAsync(c->scen_list, one.data(), sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  c->h_scen_list = one;
+  TG_TRY(tapgpu::upload_states(c, 1, max_iters, target_relgap));
+  if (x0) {
+    std::vector<double> xi(c->M);
+    for (int k = 0; k < c->M; ++k) xi[k] = x0[c->perm[k]];
+    TG_CUDA(cudaMemcpyAsync(c->x, xi.data(), sizeof(double) * c->M, cudaMemcpyHostToDevice,
+                            c->stream));
+    TG_CUDA(cudaStreamSynchronize(c->stream));
+  }
+  TG_TRY(c->enqueue_initial(1, x0 != nullptr));
+  TG_TRY(c->sync_check());
+  c->solve_max_iters = max_iters;
+  return TAPGPU_OK;
+}
+
+int tapgpu_solve_advance(tapgpu_ctx* ctx, int max_new_iters, int* done, tapgpu_result* res) {
+  if (!ctx || max_new_iters < 1) return TAPGPU_ERR_ARG;
+  Ctx* c = ctx->c;
+  TG_CUDA(cudaSetDevice(c->device));
+  std::vector<tapgpu::ScenState> st;
+  TG_TRY(c->read_states(1, st));
+  if (!st[0].done) {
+    int n = max_new_iters;
+    if (c->solve_max_iters > 0) n = std::max(1, std::min(n, c->solve_max_iters - st[0].iter));
+    TG_TRY(c->run_graph(n, 1));
+    TG_TRY(c->read_states(1, st));
+  }
+  TG_TRY(c->sync_check());
+  int e = 0;
+  TG_CUDA(cudaMemcpy(&e, c->err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (done) *done = st[0].done;
+  if (res) tapgpu::fill_result(st[0], e, res);
+  return TAPGPU_OK;
+}
+
+int tapgpu_solve(tapgpu_ctx* ctx, int max_iters, double target_relgap, const double* x0,
+                 tapgpu_result* res) {
+  int rc = tapgpu_solve_begin(ctx, max_iters, target_relgap, x0);
+  if (rc != TAPGPU_OK) return rc;
+  Ctx* c = ctx->c;
+  std::vector<tapgpu::ScenState> st;
+  TG_TRY(tapgpu::iterate_until_done(c, 1, max_iters, st));
+  int e = 0;
+  TG_CUDA(cudaMemcpy(&e, c->err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (res) tapgpu::fill_result(st[0], e, res);
+  return TAPGPU_OK;
+}
+
+int tapgpu_get_link_flows(tapgpu_ctx* ctx, int scenario, double* volume, double* cost) {
+  if (!ctx) return TAPGPU_ERR_ARG;
+  Ctx* c = ctx->c;
+  if (scenario < 0 || scenario >= c->S_cap) return TAPGPU_ERR_ARG;
+  TG_CUDA(cudaSetDevice(c->device));
+  TG_CUDA(cudaStreamSynchronize(c->stream));
+  std::vector<double> tmp(c->M);
+  const size_t off = static_cast<size_t>(scenario) * c->M;
+  if (volume) {
+    TG_CUDA(cudaMemcpy(tmp.data(), c->x + off, sizeof(double) * c->M, cudaMemcpyDeviceToHost));
+    for (int k = 0; k < c->M; ++k) volume[c->perm[k]] = tmp[k];
+  }
+  if (cost) {
+    TG_CUDA(cudaMemcpy(tmp.data(), c->t + off, sizeof(double) * c->M, cudaMemcpyDeviceToHost));
+    for (int k = 0; k < c->M; ++k) cost[c->perm[k]] = tmp[k];
+  }
+  return TAPGPU_OK;
+}
+
+int tapgpu_get_trace(tapgpu_ctx* ctx, int scenario, double* rows, int max_rows, int* nrows) {
+  if (!ctx || !rows || !nrows) return TAPGPU_ERR_ARG;
+  Ctx* c = ctx->c;
+  if (scenario < 0 || scenario >= c->S_cap) return TAPGPU_ERR_ARG;
+  TG_CUDA(cudaSetDevice(c->device));
+  tapgpu::ScenState st;
+  TG_CUDA(cudaStreamSynchronize(c->stream));
+  TG_CUDA(cudaMemcpy(&st, c->state + scenario, sizeof(st), cudaMemcpyDeviceToHost));
+  const int n = std::min(std::min(st.iter, c->trace_cap), max_rows);
+  if (n > 0)
+    TG_CUDA(cudaMemcpy(rows, c->trace + static_cast<size_t>(scenario) * c->trace_cap * tapgpu::kTraceCols,
+                       sizeof(double) * n * tapgpu::kTraceCols, cudaMemcpyDeviceToHost));
+  *nrows = n;
+  return TAPGPU_OK;
+}
+
+int tapgpu_solve_scenarios(tapgpu_ctx* ctx, int num_scen, const int64_t* scen_ptr,
+                           const int64_t* scen_links, const double* scen_cap, int max_iters,
+                           double target_relgap, const double* x0, tapgpu_result* results) {
+  if (!ctx || num_scen < 1 || !scen_ptr || (max_iters <= 0 && !(target_relgap > 0))) {
+    tapgpu::set_message("bad scenario arguments");
+    return TAPGPU_ERR_ARG;
+  }
+  Ctx* c = ctx->c;
+  const int M = c->M;
+  std::vector<int64_t> inv(M);
+  for (int k = 0; k < M; ++k) inv[c->perm[k]] = k;
+  for (int s = 0; s < num_scen; ++s) {
+    if (scen_ptr[s + 1] < scen_ptr[s]) return TAPGPU_ERR_ARG;
+    for (int64_t i = scen_ptr[s]; i < scen_ptr[s + 1]; ++i)
+      if (scen_links[i] < 0 || scen_links[i] >= M || std::isnan(scen_cap[i])) {
+        tapgpu::set_message("scenario link index out of range");
+        return TAPGPU_ERR_ARG;
+      }
+  }
+  TG_CUDA(cudaSetDevice(c->device));
+  TG_TRY(c->ensure_scenarios(num_scen));
+  // capacities of every scenario: base with the scenario's edits
+  std::vector<double> caps(static_cast<size_t>(num_scen) * M);
+  for (int s = 0; s < num_scen; ++s) {
+    double* row = caps.data() + static_cast<size_t>(s) * M;
+    std::copy(c->h_cap.begin(), c->h_cap.end(), row);
+    for (int64_t i = scen_ptr[s]; i < scen_ptr[s + 1]; ++i) {
+      const double v = scen_cap[i];
+      row[inv[scen_links[i]]] = v;
+    }
+    double mn = DBL_MAX;
+    for (int k = 0; k < M; ++k)
+      if (row[k] > 0 && row[k] < mn) mn = row[k];
+    for (int k = 0; k < M; ++k)
+      if (!(row[k] > 0)) row[k] = mn;
+  }
+  TG_CUDA(cudaMemcpyAsync(c->cap, caps.data(), sizeof(double) * caps.size(),
+                          cudaMemcpyHostToDevice, c->stream));
+  std::vector<int> all(num_scen);
+  std::iota(all.begin(), all.end(), 0);
+  TG_CUDA(cudaMemcpyAsync(c->scen_list, all.data(), sizeof(int) * num_scen,
+                          cudaMemcpyHostToDevice, c->stream));
+  c->h_scen_list = all;
+  TG_TRY(tapgpu::upload_states(c, num_scen, max_iters, target_relgap));
+  if (x0) {
+    std::vector<double> xi(M);
+    for (int k = 0; k < M; ++k) xi[k] = x0[c->perm[k]];
+    for (int s = 0; s < num_scen; ++s)
+      TG_CUDA(cudaMemcpyAsync(c->x + static_cast<size_t>(s) * M, xi.data(), sizeof(double) * M,
+                              cudaMemcpyHostToDevice, c->stream));
+    TG_CUDA(cudaStreamSynchronize(c->stream));
+    TG_TRY(c->enqueue_initial(num_scen, true));
+  } else {
+    // free-flow all-or-nothing does not depend on capacity: load scenario 0
+    // once and start every scenario from it
+    tapgpu::LinkArgs la = c->link_args(1);
+    TG_CUDA(tapgpu::launch_set_costs(la, c->link_grid, c->stream));
+    TG_TRY(c->enqueue_paths(1, true, c->w32, c->w64, c->yfx, true));
+    for (int s = 1; s < num_scen; ++s)
+      TG_CUDA(cudaMemcpyAsync(c->yfx + static_cast<size_t>(s) * M, c->yfx,
+                              sizeof(unsigned long long) * M, cudaMemcpyDeviceToDevice,
+                              c->stream));
+    la = c->link_args(num_scen);
+    la.pass = 0;
+    TG_CUDA(tapgpu::launch_init_flows(la, c->link_grid, c->stream));
+  }
+  TG_TRY(c->sync_check());
+  std::vector<tapgpu::ScenState> st;
+  TG_TRY(tapgpu::iterate_until_done(c, num_scen, max_iters, st));
+  int e = 0;
+  TG_CUDA(cudaMemcpy(&e, c->err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (results)
+    for (int s = 0; s < num_scen; ++s) tapgpu::fill_result(st[s], e, &results[s]);
+  return TAPGPU_OK;
+}
+
+static int to_device_weights(Ctx* c, const double* weights) {
+  std::vector<double> w(c->M);
+  std::vector<float> wf(c->M);
+  for (int k = 0; k < c->M; ++k) {
+    const double v = weights[c->perm[k]];
+    if (!(v >= 0) || std::isinf(v)) {
+      tapgpu::set_message("link costs must be finite and non-negative");
+      return TAPGPU_ERR_ARG;
+    }
+    w[k] = v;
+    wf[k] = static_cast<float>(v);
+  }
+  TG_CUDA(cudaMemcpyAsync(c->api_w64, w.data(), sizeof(double) * c->M, cudaMemcpyHostToDevice,
+                          c->stream));
+  TG_CUDA(cudaMemcpyAsync(c->api_w32, wf.data(), sizeof(float) * c->M, cudaMemcpyHostToDevice,
+                          c->stream));
+  TG_CUDA(cudaStreamSynchronize(c->stream));
+  return TAPGPU_OK;
+}
+
+int tapgpu_sssp(tapgpu_ctx* ctx, const double* weights, const int64_t* srcs, int64_t num_sources,
+                double* dist, int64_t* pred) {
+  if (!ctx || !weights || (num_sources > 0 && !srcs)) return TAPGPU_ERR_ARG;
+  Ctx* c = ctx->c;
+  for (int64_t i = 0; i < num_sources; ++i)
+    if (srcs[i] < 0 || srcs[i] >= c->n1) {
+      tapgpu::set_message("source node out of range");
+      return TAPGPU_ERR_ARG;
+    }
+  TG_CUDA(cudaSetDevice(c->device));
+  TG_TRY(to_device_weights(c, weights));
+  const int n1 = c->n1;
+  if (!c->pred_buf) TG_TRY(c->alloc_n(&c->pred_buf, static_cast<size_t>(c->dist_tasks) * n1));
+  int* dsrc = nullptr;
+  // FP64 labels: a FP32 context's label buffer holds half as many sources
+  const int64_t chunk = c->fp64 ? c->dist_tasks : std::max<int64_t>(1, c->dist_tasks / 2);
+  TG_TRY(c->alloc_n(&dsrc, static_cast<size_t>(std::max<int64_t>(1, std::min(chunk, num_sources)))));
+  std::vector<double> dtmp;
+  std::vector<float> ftmp;
+  std::vector<int> ptmp;
+  int rc = TAPGPU_OK;
+  // the API always computes FP64 labels: they equal the reference's bit for bit
+  for (int64_t s0 = 0; s0 < num_sources && rc == TAPGPU_OK; s0 += chunk) {
+    const int64_t s1 = std::min(num_sources, s0 + chunk);
+    const int ns = static_cast<int>(s1 - s0);
+    std::vector<int> hs(ns);
+    for (int i = 0; i < ns; ++i) hs[i] = static_cast<int>(srcs[s0 + i]);
+    if (cudaMemcpyAsync(dsrc, hs.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, c->stream) !=
+        cudaSuccess) {
+      rc = TAPGPU_ERR_CUDA;
+      break;
+    }
+    tapgpu::PathArgs a = c->path_args(1);
+    a.sources = dsrc;
+    a.num_sources = ns;
+    a.scen_list = nullptr;
+    a.state = nullptr;
+    a.task_begin = 0;
+    a.task_end = ns;
+    a.w64 = c->api_w64;
+    a.w32 = nullptr;
+    a.do_load = 0;
+    a.pred_out = c->pred_buf;
+    a.y_fx = c->api_yfx;
+    const int optin = tapgpu::max_smem_optin(c->device);
+    const bool s_smem = tapgpu::sssp_smem_bytes(n1, true) + 1024 <= static_cast<size_t>(optin);
+    const int occ = tapgpu::sssp_occupancy(true, c->sssp_block, s_smem, n1);
+    int grid = std::max(1, std::min(occ * c->num_sms, ns));
+    if (!s_smem) {
+      const size_t need = tapgpu::sssp_smem_bytes(n1, true) * static_cast<size_t>(grid);
+      if (need > c->path_scratch_bytes) {
+        grid = std::max<int>(1, static_cast<int>(c->path_scratch_bytes / tapgpu::sssp_smem_bytes(n1, true)));
+        if (c->path_scratch_bytes == 0) {
+          rc = TAPGPU_ERR_UNSUPPORTED;
+          break;
+        }
+      }
+    }
+    cudaMemsetAsync(c->counters, 0, 2 * sizeof(int), c->stream);
+    a.counter = c->counters;
+    a.scratch_stride = static_cast<long long>(tapgpu::sssp_smem_bytes(n1, true));
+    if (tapgpu::launch_sssp(a, true, grid, c->sssp_block, s_smem, c->stream) != cudaSuccess) {
+      rc = TAPGPU_ERR_CUDA;
+      break;
+    }
+    a.counter = c->counters + 1;
+    a.scratch_stride = static_cast<long long>(tapgpu::aon_smem_bytes(n1));
+    if (tapgpu::launch_aon(a, true, std::min(c->aon_grid, ns), c->aon_block, c->aon_smem,
+                           c->stream) != cudaSuccess) {
+      rc = TAPGPU_ERR_CUDA;
+      break;
+    }
+    rc = c->sync_check();
+    if (rc != TAPGPU_OK) break;
+    if (dist) {
+      dtmp.resize(static_cast<size_t>(ns) * n1);
+      if (cudaMemcpy(dtmp.data(), c->dist, sizeof(double) * dtmp.size(), cudaMemcpyDeviceToHost) !=
+          cudaSuccess) {
+        rc = TAPGPU_ERR_CUDA;
+        break;
+      }
+      for (size_t i = 0; i < dtmp.size(); ++i)
+        dist[static_cast<size_t>(s0) * n1 + i] = std::isinf(dtmp[i]) ? DBL_MAX : dtmp[i];
+    }
+    if (pred) {
+      ptmp.resize(static_cast<size_t>(ns) * n1);
+      if (cudaMemcpy(ptmp.data(), c->pred_buf, sizeof(int) * ptmp.size(), cudaMemcpyDeviceToHost) !=
+          cudaSuccess) {
+        rc = TAPGPU_ERR_CUDA;
+        break;
+      }
+      for (size_t i = 0; i < ptmp.size(); ++i)
+        pred[static_cast<size_t>(s0) * n1 + i] = ptmp[i] >= 0 ? c->perm[ptmp[i]] : -1;
+    }
+  }
+  tapgpu::free_owned(c, dsrc);
+  if (rc == TAPGPU_ERR_CUDA && tapgpu::g_message.empty())
+    tapgpu::set_message(cudaGetErrorString(cudaGetLastError()));
+  return rc;
+}
+
+int tapgpu_aon(tapgpu_ctx* ctx, const double* weights, double* volume) {
+  if (!ctx || !weights || !volume) return TAPGPU_ERR_ARG;
+  Ctx* c = ctx->c;
+  TG_CUDA(cudaSetDevice(c->device));
+  TG_TRY(to_device_weights(c, weights));
+  TG_CUDA(cudaMemsetAsync(c->api_yfx, 0, sizeof(unsigned long long) * c->M, c->stream));
+  TG_CUDA(cudaMemsetAsync(c->err, 0, sizeof(int), c->stream));
+  TG_TRY(c->enqueue_paths(1, true, c->fp64 ? nullptr : c->api_w32, c->fp64 ? c->api_w64 : nullptr,
+                          c->api_yfx, false));
+  TG_TRY(c->sync_check());
+  std::vector<unsigned long long> y(c->M);
+  TG_CUDA(cudaMemcpy(y.data(), c->api_yfx, sizeof(unsigned long long) * c->M,
+                     cudaMemcpyDeviceToHost));
+  for (int k = 0; k < c->M; ++k)
+    volume[c->perm[k]] = static_cast<double>(static_cast<long long>(y[k])) * c->inv_scale;
+  return TAPGPU_OK;
+}
+
+void* tapgpu_stream(tapgpu_ctx* ctx) { return ctx ? ctx->c->stream : nullptr; }
+
+int tapgpu_run_iterations(tapgpu_ctx* ctx, int iters) {
+  if (!ctx || iters < 1) return TAPGPU_ERR_ARG;
+  Ctx* c = ctx->c;
+  TG_CUDA(cudaSetDevice(c->device));
+  std::vector<tapgpu::ScenState> st;
+  TG_TRY(c->read_states(1, st));
+  st[0].done = 0;
+  st[0].max_iters = st[0].iter + iters;
+  st[0].target_relgap = 0.0;
+  TG_CUDA(cudaMemcpyAsync(c->state, st.data(), sizeof(tapgpu::ScenState), cudaMemcpyHostToDevice,
+                          c->stream));
+  std::vector<int> one{0};
+  if (c->h_scen_list != one) {
+    TG_CUDA(cudaMemcpyAsync(c->scen_list, one.data(), sizeof(int), cudaMemcpyHostToDevice,
+                            c->stream));
+    c->h_scen_list = one;
+  }
+  TG_TRY(c->run_graph(iters, 1));
+  return TAPGPU_OK;
+}
+
+int tapgpu_profile_iteration(tapgpu_ctx* ctx, int reps, float* ms) {
+  if (!ctx || !ms || reps < 1) return TAPGPU_ERR_ARG;
+  Ctx* c = ctx->c;
+  TG_CUDA(cudaSetDevice(c->device));
+  std::vector<tapgpu::ScenState> st;
+  TG_TRY(c->read_states(1, st));
+  st[0].done = 0;
+  st[0].max_iters = 0;
+  st[0].target_relgap = 0.0;
+  TG_CUDA(cudaMemcpyAsync(c->state, st.data(), sizeof(tapgpu::ScenState), cudaMemcpyHostToDevice,
+                          c->stream));
+  std::vector<int> one{0};
+  TG_CUDA(cudaMemcpyAsync(c->scen_list, one.data(), sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  c->h_scen_list = one;
+  cudaEvent_t ev[5];
+  for (auto& e : ev) TG_CUDA(cudaEventCreate(&e));
+  double acc[5] = {0, 0, 0, 0, 0};
+  int rc = TAPGPU_OK;
+  for (int r = 0; r < reps && rc == TAPGPU_OK; ++r) {
+    cudaEventRecord(ev[0], c->stream);
+    const int64_t tasks = c->Z;
+    tapgpu::PathArgs a = c->path_args(1);
+    a.task_end = static_cast<int>(tasks);
+    cudaMemsetAsync(c->counters, 0, 2 * sizeof(int), c->stream);
+    a.counter = c->counters;
+    a.scratch_stride = static_cast<long long>(tapgpu::sssp_smem_bytes(c->n1, c->fp64));
+    a.w32 = c->fp64 ? nullptr : c->w32;
+    a.w64 = c->fp64 ? c->w64 : nullptr;
+    if (tasks > c->dist_tasks) {
+      rc = TAPGPU_ERR_UNSUPPORTED;
+      break;
+    }
+    tapgpu::launch_sssp(a, c->fp64, std::min<int64_t>(c->sssp_grid, tasks), c->sssp_block,
+                        c->sssp_smem, c->stream);
+    cudaEventRecord(ev[1], c->stream);
+    a.counter = c->counters + 1;
+    a.scratch_stride = static_cast<long long>(tapgpu::aon_smem_bytes(c->n1));
+    tapgpu::launch_aon(a, c->fp64, std::min<int64_t>(c->aon_grid, tasks), c->aon_block,
+                       c->aon_smem, c->stream);
+    cudaEventRecord(ev[2], c->stream);
+    tapgpu::LinkArgs la = c->link_args(1);
+    for (int p = 0; p < tapgpu::kLsPasses; ++p) {
+      la.pass = p;
+      tapgpu::launch_ls_pass(la, c->link_grid, c->stream);
+    }
+    tapgpu::launch_ls_fallback(la, c->stream);
+    cudaEventRecord(ev[3], c->stream);
+    tapgpu::launch_step(la, c->link_grid, c->stream);
+    cudaEventRecord(ev[4], c->stream);
+    if (cudaEventSynchronize(ev[4]) != cudaSuccess) {
+      rc = TAPGPU_ERR_CUDA;
+      break;
+    }
+    float t;
+    for (int i = 0; i < 4; ++i) {
+      cudaEventElapsedTime(&t, ev[i], ev[i + 1]);
+      acc[i] += t;
+    }
+    cudaEventElapsedTime(&t, ev[0], ev[4]);
+    acc[4] += t;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (rc != TAPGPU_OK) return rc;
+  TG_TRY(c->sync_check());
+  for (int i = 0; i < 5; ++i) ms[i] = static_cast<float>(acc[i] / reps);
+  return TAPGPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,112 @@
+// solver.cuh - host-side solver context behind the tapgpu_* C ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "fw_kernels.cuh"
+#include "tap_gpu.h"
+
+namespace tapgpu {
+
+void set_message(const std::string& m);
+
+// device allocation owned by a context
+struct DevMem {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+struct Ctx {
+  // sizes (internal link order: sorted by (init, term))
+  int N = 0, n1 = 0, M = 0, Z = 0, F = 0;
+  bool fp64 = true;
+  int device = 0, num_sms = 0;
+  tapgpu_options opt{};
+  std::vector<int64_t> perm;  // internal link k -> caller's link index
+  std::vector<int> h_tail, h_head;
+  std::vector<double> h_cap, h_fft, h_alpha, h_beta;
+
+  // device topology and link parameters
+  int *row_ptr = nullptr, *head = nullptr, *tail = nullptr, *in_ptr = nullptr, *in_link = nullptr;
+  double *fft = nullptr, *alpha = nullptr, *beta = nullptr;
+  unsigned char* ipow = nullptr;
+
+  // demand
+  int *od_ptr = nullptr, *od_dest = nullptr;
+  long long* od_q = nullptr;
+  double* od_dem = nullptr;
+  int* sources = nullptr;
+  double inv_scale = 1.0, total_demand = 0.0;
+  int scale_bits = 0;
+
+  // per-scenario state (capacity for S_cap scenarios)
+  int S_cap = 0;
+  double *cap = nullptr, *x = nullptr, *t = nullptr, *d = nullptr, *dtdx = nullptr;
+  unsigned long long* yfx = nullptr;
+  float* w32 = nullptr;
+  double* w64 = nullptr;
+  ScenState* state = nullptr;
+  double* partials = nullptr;
+  unsigned* arrive = nullptr;
+  double* trace = nullptr;
+  int trace_cap = 0;
+  int* scen_list = nullptr;
+  std::vector<int> h_scen_list;
+  double *x_hist = nullptr, *d_hist = nullptr, *lam_hist = nullptr;
+  int hist_cap = 0;
+
+  // scratch
+  void* dist = nullptr;
+  int64_t dist_tasks = 0;  // tasks the dist buffer holds
+  void* path_scratch = nullptr;
+  size_t path_scratch_bytes = 0;
+  int* counters = nullptr;  // [2]
+  int* err = nullptr;       // [1]
+  int* err_info = nullptr;  // [2]
+  int* pred_buf = nullptr;  // [dist_tasks][n1] for the shortest-path API
+  // buffers of the one-shot API (weights in both precisions, loaded volumes)
+  float* api_w32 = nullptr;
+  double* api_w64 = nullptr;
+  unsigned long long* api_yfx = nullptr;
+
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int g_iters = 0, g_nscen = -1;
+  int solve_max_iters = 0;
+
+  // launch shapes
+  int sssp_block = 256, aon_block = 512, link_grid = 0;
+  bool sssp_smem = true, aon_smem = true;
+  int sssp_grid = 0, aon_grid = 0;
+
+  std::vector<DevMem> owned;
+
+  ~Ctx();
+  int alloc(void** p, size_t bytes);
+  template <class T>
+  int alloc_n(T** p, size_t n) {
+    return alloc(reinterpret_cast<void**>(p), n * sizeof(T));
+  }
+  int ensure_scenarios(int S);
+  int plan_launches();
+
+  Graph graph() const;
+  LinkParams link_params() const;
+  Demand demand() const;
+  PathArgs path_args(int nscen_slots) const;
+  LinkArgs link_args(int nscen) const;
+
+  // enqueue helpers (stream ordered, capturable)
+  int enqueue_paths(int nscen, bool load, const float* w32p, const double* w64p,
+                    unsigned long long* ydst, bool use_state);
+  int enqueue_iteration(int nscen);
+  int enqueue_initial(int nscen, bool warm);
+  int run_graph(int iters, int nscen);
+  int sync_check();
+  int read_states(int S, std::vector<ScenState>& out);
+};
+
+}  // namespace tapgpu

@@ -1,0 +1,186 @@
+"""Python front end of the GPU Frank-Wolfe solver (handle API of include/tap_gpu.h)."""
+
+from __future__ import annotations
+
+import ctypes as C
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+
+from . import _capi as K
+from .synth import Demand, Network, Scenario
+
+__all__ = ["Solver", "SolveResult"]
+
+
+class SolveResult(dict):
+    """iterations, error_bits, objective, relgap, total_cost, avg_excess, lambda_last."""
+
+    def __getattr__(self, k):
+        try:
+            return self[k]
+        except KeyError as e:
+            raise AttributeError(k) from e
+
+
+def _net_struct(net: Network, keep: list):
+    arrs = [np.ascontiguousarray(net.init, np.int64), np.ascontiguousarray(net.term, np.int64),
+            np.ascontiguousarray(net.capacity, np.float64),
+            np.ascontiguousarray(net.fft, np.float64),
+            np.ascontiguousarray(net.alpha, np.float64),
+            np.ascontiguousarray(net.beta, np.float64)]
+    keep.extend(arrs)
+    return K.Network(net.num_nodes, net.num_zones, net.first_thru_node, net.num_links,
+                     K.ptr(arrs[0], K.I64P), K.ptr(arrs[1], K.I64P), K.ptr(arrs[2], K.F64P),
+                     K.ptr(arrs[3], K.F64P), K.ptr(arrs[4], K.F64P), K.ptr(arrs[5], K.F64P))
+
+
+def _dem_struct(dem: Demand, keep: list):
+    arrs = [np.ascontiguousarray(dem.od_ptr, np.int64), np.ascontiguousarray(dem.od_dest, np.int64),
+            np.ascontiguousarray(dem.od_demand, np.float64)]
+    if arrs[1].size == 0:
+        arrs[1] = np.zeros(1, np.int64)
+        arrs[2] = np.zeros(1)
+    keep.extend(arrs)
+    return K.DemandS(dem.num_zones, K.ptr(arrs[0], K.I64P), K.ptr(arrs[1], K.I64P),
+                     K.ptr(arrs[2], K.F64P))
+
+
+class Solver:
+    """One network + demand on one GPU.
+
+    precision: "fp64" (all-FP64 shortest paths, parity with the reference) or
+    "fp32" (FP32 path costs; gap, objective, line search and VHT stay FP64).
+    """
+
+    def __init__(self, net: Network, dem: Optional[Demand] = None, precision: str = "fp64",
+                 device: int = 0, sssp_block: int = 0, aon_block: int = 0,
+                 iters_per_launch: int = 0, use_graphs: bool = True, chunk_tasks: int = 0,
+                 record_tape: bool = False, tape_capacity: int = 0):
+        self.L = K.load()
+        self.net = net
+        self.dem = dem
+        opt = K.Options()
+        self.L.tapgpu_default_options(C.byref(opt))
+        opt.precision = K.TAPGPU_FP32_PATHS if precision in ("fp32", "fp32path") else K.TAPGPU_FP64
+        opt.device = device
+        opt.sssp_block = sssp_block
+        opt.aon_block = aon_block
+        opt.iters_per_launch = iters_per_launch
+        opt.use_graphs = 1 if use_graphs else 0
+        opt.chunk_tasks = chunk_tasks
+        opt.record_tape = 1 if record_tape else 0
+        opt.tape_capacity = tape_capacity
+        self.precision = "fp32" if opt.precision == K.TAPGPU_FP32_PATHS else "fp64"
+        keep: list = []
+        ns = _net_struct(net, keep)
+        ds = _dem_struct(dem, keep) if dem is not None else None
+        h = C.c_void_p()
+        K.check(self.L.tapgpu_create(C.byref(ns), C.byref(ds) if ds is not None else None,
+                                     C.byref(opt), C.byref(h)))
+        self.h = h
+        self.m = net.num_links
+        self.n1 = net.num_nodes + 1
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.L.tapgpu_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ------------------------------------------------------------------
+    def solve(self, max_iters: int = 0, target_relgap: float = 0.0,
+              x0: Optional[np.ndarray] = None) -> SolveResult:
+        r = K.Result()
+        xa = None if x0 is None else np.ascontiguousarray(x0, np.float64)
+        K.check(self.L.tapgpu_solve(self.h, int(max_iters), float(target_relgap),
+                                    None if xa is None else K.ptr(xa, K.F64P), C.byref(r)))
+        return SolveResult(r.as_dict())
+
+    def begin(self, max_iters: int = 0, target_relgap: float = 0.0,
+              x0: Optional[np.ndarray] = None):
+        xa = None if x0 is None else np.ascontiguousarray(x0, np.float64)
+        K.check(self.L.tapgpu_solve_begin(self.h, int(max_iters), float(target_relgap),
+                                          None if xa is None else K.ptr(xa, K.F64P)))
+
+    def advance(self, iters: int):
+        r = K.Result()
+        done = C.c_int(0)
+        K.check(self.L.tapgpu_solve_advance(self.h, int(iters), C.byref(done), C.byref(r)))
+        return bool(done.value), SolveResult(r.as_dict())
+
+    def flows(self, scenario: int = 0):
+        v = np.zeros(self.m)
+        t = np.zeros(self.m)
+        K.check(self.L.tapgpu_get_link_flows(self.h, scenario, K.ptr(v, K.F64P), K.ptr(t, K.F64P)))
+        return v, t
+
+    def trace(self, scenario: int = 0, max_rows: int = 1000000) -> np.ndarray:
+        """Rows: objective, relgap, avg_excess, vht, lambda, gap, iter, g0."""
+        n = C.c_int(0)
+        rows = np.zeros((max_rows, K.TRACE_COLS))
+        K.check(self.L.tapgpu_get_trace(self.h, scenario, K.ptr(rows, K.F64P), max_rows,
+                                        C.byref(n)))
+        return rows[: n.value].copy()
+
+    def set_capacity(self, cap: np.ndarray):
+        ca = np.ascontiguousarray(cap, np.float64)
+        K.check(self.L.tapgpu_set_capacity(self.h, K.ptr(ca, K.F64P)))
+
+    def sssp(self, weights: np.ndarray, sources: Sequence[int], want_dist=True, want_pred=True):
+        w = np.ascontiguousarray(weights, np.float64)
+        src = np.ascontiguousarray(sources, np.int64)
+        d = np.zeros((len(src), self.n1)) if want_dist else None
+        p = np.zeros((len(src), self.n1), np.int64) if want_pred else None
+        K.check(self.L.tapgpu_sssp(self.h, K.ptr(w, K.F64P), K.ptr(src, K.I64P), len(src),
+                                   None if d is None else K.ptr(d, K.F64P),
+                                   None if p is None else K.ptr(p, K.I64P)))
+        return d, p
+
+    def aon(self, weights: np.ndarray) -> np.ndarray:
+        w = np.ascontiguousarray(weights, np.float64)
+        y = np.zeros(self.m)
+        K.check(self.L.tapgpu_aon(self.h, K.ptr(w, K.F64P), K.ptr(y, K.F64P)))
+        return y
+
+    def solve_scenarios(self, scenarios: List[Scenario], max_iters: int = 0,
+                        target_relgap: float = 0.0, x0: Optional[np.ndarray] = None):
+        ptr = [0]
+        links, caps = [], []
+        for sc in scenarios:
+            links.extend(np.asarray(sc.links, np.int64).tolist())
+            caps.extend(np.asarray(sc.new_capacity, np.float64).tolist())
+            ptr.append(len(links))
+        pa = np.asarray(ptr, np.int64)
+        la = np.asarray(links if links else [0], np.int64)
+        ca = np.asarray(caps if caps else [0.0], np.float64)
+        res = (K.Result * len(scenarios))()
+        xa = None if x0 is None else np.ascontiguousarray(x0, np.float64)
+        K.check(self.L.tapgpu_solve_scenarios(self.h, len(scenarios), K.ptr(pa, K.I64P),
+                                              K.ptr(la, K.I64P), K.ptr(ca, K.F64P),
+                                              int(max_iters), float(target_relgap),
+                                              None if xa is None else K.ptr(xa, K.F64P), res))
+        return [SolveResult(r.as_dict()) for r in res]
+
+    def stream_ptr(self) -> int:
+        return int(self.L.tapgpu_stream(self.h) or 0)
+
+    def run_iterations(self, iters: int):
+        K.check(self.L.tapgpu_run_iterations(self.h, int(iters)))
+
+    def profile_iteration(self, reps: int = 5) -> Dict[str, float]:
+        ms = (C.c_float * 5)()
+        K.check(self.L.tapgpu_profile_iteration(self.h, int(reps), ms))
+        return dict(sssp_ms=ms[0], aon_ms=ms[1], line_search_ms=ms[2], step_ms=ms[3],
+                    iteration_ms=ms[4])
