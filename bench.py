@@ -1,0 +1,379 @@
+"""Benchmark: FW iterations/sec and scenarios/sec, batched FP32-path vs plain, 1 GB300.
+
+Workload (both arms): the 10,000-node synthetic network (100 x 100 perturbed
+grid + 200 two-way arterials, 40,000 links, 1,000 zones, gravity demand of
+1.5M trips/h, BPR 0.15/4) with 256 upgrade scenarios (capacity +25-100% on
+1-20 random links).  A *step* is one Frank-Wolfe iteration of all 256
+scenarios in one batched launch sequence (FP32 path costs, FP64 gap /
+objective / line search / VHT).  ``value`` is scenario-iterations per second
+with everything resident in HBM; ``e2e`` is the same metric through the C ABI
+call tapgpu_solve_scenarios from host buffers (capacities and warm-start
+flows in, every scenario's flows and costs out).
+
+Also reported: scenarios/sec to relative gap 1e-4 for the batched solver and
+for the plain single-scenario GPU path, the roofline of the dominant kernel
+(all-origins shortest paths), per-kernel times measured with CUDA events on
+the solver's stream, SM clocks sampled during the timed region, and the CPU
+baseline (the oracle's pthread Frank-Wolfe on the host cores).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "FW iters/sec and scenarios/sec to rel-gap 1e-4, batched FP32 vs plain, 1 GB300"
+UNIT = "scenario-FW-iterations/s"
+WORKLOAD = ("grid10k x 256 upgrade scenarios: 10,000 nodes, 40,000 links, 1,000 zones, "
+            "gravity OD 1.5M trips/h, BPR alpha 0.15 beta 4, batched FW iteration, FP32 paths")
+
+
+def _env_rank():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+class Dist:
+    """Barrier and max-over-ranks for timing only (no data-path collective)."""
+
+    def __init__(self, world):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as td
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, v):
+        if self.world == 1:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v):
+        if self.world == 1:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.idx = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for i, n in enumerate(names):
+                if len(r) > 5 + i and r[5 + i].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.rows)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0}, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per full shortest-path launch, from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "k_sssp_grid10k.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_full_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_baseline(net, dem, scen, seconds=15.0):
+    """The oracle's pthread FW (the reference's algorithm) on all host cores:
+    FW iterations of one upgrade scenario, iterated until ~`seconds` elapse."""
+    import oracle
+    cores = os.cpu_count() or 1
+    cap = net.capacity.copy()
+    cap[scen.links] = scen.new_capacity
+    t0 = time.perf_counter()
+    it = 1
+    while True:
+        r = oracle.frankwolfe(net, dem, threads=cores, max_iters=it, capacity=cap)
+        el = time.perf_counter() - t0
+        if el >= seconds or it >= 64:
+            break
+        it *= 2
+    # per-iteration time from the solver's own per-iteration wall clock
+    ms = r["trace"][:, 6]
+    per_iter = float(np.mean(ms)) / 1e3
+    return {"value": 1.0 / per_iter, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"grid10k, 1 upgrade scenario, {len(ms)} FW iterations (oracle pthread "
+                      f"FW on {cores} host threads, per-iteration wall clock)"}
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the reference's CPU algorithm (oracle port, all host
+    threads) on the same workload; each step is one FW iteration of one
+    upgrade scenario."""
+    if rank != 0:
+        return 0
+    import oracle
+    from traffic_assignment_gb300 import synth
+    net, dem = synth.make_grid10k()
+    scen = synth.make_scenarios(net, 256)[0]
+    cap = net.capacity.copy()
+    cap[scen.links] = scen.new_capacity
+    cores = os.cpu_count() or 1
+    total = args.warmup + args.steps
+    r = oracle.frankwolfe(net, dem, threads=cores, max_iters=total, capacity=cap)
+    ms = r["trace"][:, 6]
+    timed = ms[args.warmup:]
+    t = float(np.sum(timed)) / 1e3
+    value = len(timed) / t
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / len(timed),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "step": "one FW iteration of one upgrade scenario "
+                       "(the reference solves scenarios one at a time)", "threads": cores},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{len(timed)} FW iterations of scenario s0000 after "
+                                       f"{args.warmup} warm-up iterations"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+
+    from traffic_assignment_gb300 import Solver, synth
+
+    dist = Dist(world)
+    torch.cuda.set_device(local_rank)
+    net, dem = synth.make_grid10k()
+    S = args.scenarios
+    # each rank solves its own scenario set (weak scaling: no data exchange)
+    scen = synth.make_scenarios(net, S, seed=1004 + 7919 * rank)
+    solver = Solver(net, dem, precision="fp32", device=local_rank)
+
+    # base equilibrium: the warm start of every scenario
+    t0 = time.perf_counter()
+    base = solver.solve(target_relgap=args.base_relgap, max_iters=args.base_max_iters)
+    xb, _ = solver.flows()
+    base_s = time.perf_counter() - t0
+
+    # plain single-scenario path: a few scenarios one at a time to rel-gap 1e-4
+    plain_n = min(args.plain_scenarios, S)
+    t0 = time.perf_counter()
+    plain_iters = []
+    for sc in scen[:plain_n]:
+        cap = net.capacity.copy()
+        cap[sc.links] = sc.new_capacity
+        solver.set_capacity(cap)
+        q = solver.solve(target_relgap=1e-4, max_iters=args.max_iters, x0=xb)
+        plain_iters.append(q["iterations"])
+    plain_s = time.perf_counter() - t0
+    solver.set_capacity(net.capacity)
+    plain_sps = plain_n / plain_s
+
+    # batched: all scenarios to rel-gap 1e-4 in one solve
+    dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = solver.solve_scenarios(scen, target_relgap=1e-4, max_iters=args.max_iters, x0=xb)
+    torch.cuda.synchronize()
+    batched_s = dist.max(time.perf_counter() - t0)
+    batched_iters = [q["iterations"] for q in res]
+    batched_sps = dist.sum(S) / batched_s
+
+    # timed steps: batched FW iterations of all S scenarios (device timing)
+    solver.run_iterations(args.warmup)
+    solver.set_timing(True)
+    stream = torch.cuda.ExternalStream(solver.stream_ptr())
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clk:
+        torch.cuda.nvtx.range_push("timed_steps")
+        ev0.record(stream)
+        solver.run_iterations(args.steps)
+        ev1.record(stream)
+        ev1.synchronize()
+        torch.cuda.nvtx.range_pop()
+    torch.cuda.synchronize()
+    dist.barrier()
+    ms = dist.max(ev0.elapsed_time(ev1))
+    tm = solver.timing()
+    solver.set_timing(False)
+    value = dist.sum(S * args.steps) / (ms / 1e3)
+
+    # end to end through the C ABI from host buffers
+    torch.cuda.synchronize()
+    e2e_iters = args.steps
+    t0 = time.perf_counter()
+    res2 = solver.solve_scenarios(scen, max_iters=e2e_iters, x0=xb)
+    outs = [solver.flows(s) for s in range(S)]
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e_value = dist.sum(S * e2e_iters) / e2e_s
+    m = net.num_links
+    n_edits = sum(len(sc.links) for sc in scen)
+    h2d = S * m * 8 * 2 + n_edits * 16 + (S + 1) * 8 + m * 8
+    d2h = S * m * 16 + S * 96
+    assert len(outs) == S and all(q["error_bits"] == 0 for q in res2)
+
+    # roofline of the shortest-path kernel: Z (12 M + 8 N) bytes per scenario-iteration
+    Z, N, M = net.num_zones, net.num_nodes, m
+    tasks_per_launch = min(S * Z, solver_chunk_tasks(solver, S * Z))
+    bytes_per_launch = (tasks_per_launch / Z) * Z * (12 * M + 8 * N)
+    sssp_avg_ms = tm["sssp_ms"] / max(1, tm["sssp_launches"])
+    achieved = bytes_per_launch / (sssp_avg_ms / 1e3) / 1e9
+    peaks, peak_kind = measured_peaks()
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    traffic = profile_traffic()
+
+    line = None
+    if rank == 0:
+        clocks = clk.summary()
+        cpu = cpu_baseline(net, dem, scen[0], seconds=args.cpu_seconds) if not args.no_cpu else None
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "scenarios_per_gpu": S,
+                       "parallelism": f"scenario shards x{world} (no collective)",
+                       "l2": "working set per step ~%.1f GB (labels %d tasks x %d nodes x 4 B) "
+                             "> 129 MB L2; no flush needed" % (
+                                 S * Z * (N + 1) * 4 / 1e9, S * Z, N + 1),
+                       "reductions": "f64", "path_costs": "f32"},
+            "scenarios_per_sec": {
+                "batched": batched_sps, "plain": plain_sps * world,
+                "speedup": batched_sps / (plain_sps * world),
+                "target_relgap": 1e-4, "warm_start": f"base equilibrium (relgap "
+                f"{base['relgap']:.2e} after {base['iterations']} iterations, {base_s:.1f} s)",
+                "batched_iters_mean": float(np.mean(batched_iters)),
+                "batched_iters_max": int(np.max(batched_iters)),
+                "plain_iters_mean": float(np.mean(plain_iters)), "plain_scenarios": plain_n},
+            "kernels_ms_per_step": {k: tm[f"{k}_ms"] / args.steps
+                                    for k in ("sssp", "aon", "line_search", "step")},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "k_sssp", "peak_kind": f"{peak_kind} hbm_gbs",
+                         "algorithmic_bytes_per_launch": bytes_per_launch,
+                         "avg_launch_ms": sssp_avg_ms},
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d / e2e_iters,
+                    "d2h_bytes_per_step": d2h / e2e_iters,
+                    "call": "tapgpu_solve_scenarios(host caps, warm flows) + "
+                            "tapgpu_get_link_flows for every scenario",
+                    "iterations": e2e_iters},
+            "gpu_launches": tm["kernel_launches"],
+        }
+        print(json.dumps(line), flush=True)
+    solver.close()
+    dist.close()
+    return 0
+
+
+def solver_chunk_tasks(solver, tasks):
+    """Tasks per shortest-path launch (the label buffer holds 2 GiB by default)."""
+    per_task = (solver.n1) * (4 if solver.precision == "fp32" else 8)
+    return max(1, (2 << 30) // per_task)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--scenarios", type=int, default=256)
+    ap.add_argument("--max-iters", type=int, default=400)
+    ap.add_argument("--base-relgap", type=float, default=2e-5)
+    ap.add_argument("--base-max-iters", type=int, default=4000)
+    ap.add_argument("--plain-scenarios", type=int, default=8)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank, world, local_rank = _env_rank()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    return run_ours(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -235,6 +235,7 @@ typedef struct tapgpu_options_s {
   int64_t chunk_tasks;   /* max (scenario, origin) shortest-path tasks per chunk; 0 = auto */
   int record_tape;       /* keep per-iteration flows and directions for the adjoint */
   int tape_capacity;     /* iterations kept on the tape */
+  int global_scratch;    /* 1: per-CTA labels in global memory even when shared memory fits */
 } tapgpu_options;
 
 typedef struct tapgpu_result_s {
@@ -302,9 +303,19 @@ void *tapgpu_stream(tapgpu_ctx *ctx);
  * ms[4] whole iteration. */
 int tapgpu_profile_iteration(tapgpu_ctx *ctx, int reps, float *ms);
 
-/* Run `iters` further FW iterations of the current single-scenario state
- * without host synchronisation inside (for throughput measurement). */
+/* Run `iters` further FW iterations of every scenario of the last solve
+ * (ignoring the stopping rule), without host synchronisation in between
+ * unless kernel timing is on. */
 int tapgpu_run_iterations(tapgpu_ctx *ctx, int iters);
+
+/* Kernel timing: with `on`, CUDA events are recorded around every launch of
+ * the iteration loop (as event nodes inside the captured graphs) and their
+ * durations accumulated; turning it on or off resets the totals.
+ * tapgpu_get_timing returns total ms and launch counts per kernel group
+ * [shortest paths, loading, line search, step] and the number of kernels
+ * the solver launched since the reset. */
+int tapgpu_set_timing(tapgpu_ctx *ctx, int on);
+int tapgpu_get_timing(tapgpu_ctx *ctx, double *ms, int64_t *counts, int64_t *kernel_launches);
 
 #ifdef __cplusplus
 }

@@ -146,6 +146,33 @@ def test_warm_start(built_lib, grid416):
     assert abs(r["relgap"] - ref["relgap"]) <= RTOL64 * abs(ref["relgap"])
 
 
+@pytest.mark.parametrize("precision,global_scratch",
+                         [("fp64", False), ("fp32", False), ("fp64", True), ("fp32", True)])
+def test_medium_network_variants(built_lib, precision, global_scratch):
+    """3,600 nodes: labels and trees no longer fit the 48 KB default (opt-in
+    shared memory), and the global-memory scratch variant gives the same answer."""
+    net, dem = synth.make_grid3600()
+    ref = oracle.frankwolfe(net, dem, threads=4, max_iters=12)
+    with Solver(net, dem, precision=precision, global_scratch=global_scratch) as s:
+        r = s.solve(max_iters=12)
+        x, _ = s.flows()
+    assert r["error_bits"] == 0
+    tol = RTOL64 if precision == "fp64" else RTOL32
+    assert _rel(x, ref["x"]) < tol
+    assert abs(r["total_cost"] - ref["total_cost"]) <= tol * abs(ref["total_cost"])
+
+
+def test_no_path_is_an_error(built_lib):
+    """Positive demand between zones that cannot reach each other (zones may
+    not be passed through here) is reported, not silently dropped
+    (tap/tap_frankwolfe_pthread.c:291-298)."""
+    from traffic_assignment_gb300 import TapGpuError
+    net, dem = synth.make_grid416(first_thru_node=39)
+    with Solver(net, dem) as s:
+        with pytest.raises(TapGpuError, match="no path"):
+            s.solve(max_iters=3)
+
+
 def test_deterministic_fp32(built_lib, grid416):
     net, dem = grid416
     outs = []

@@ -45,7 +45,7 @@ class Options(C.Structure):
     _fields_ = [("precision", C.c_int), ("device", C.c_int), ("sssp_block", C.c_int),
                 ("aon_block", C.c_int), ("iters_per_launch", C.c_int), ("use_graphs", C.c_int),
                 ("chunk_tasks", C.c_int64), ("record_tape", C.c_int),
-                ("tape_capacity", C.c_int)]
+                ("tape_capacity", C.c_int), ("global_scratch", C.c_int)]
 
 
 class Result(C.Structure):
@@ -77,7 +77,8 @@ EXPORTED = [
     "tapgpu_destroy", "tapgpu_solve", "tapgpu_solve_begin", "tapgpu_solve_advance",
     "tapgpu_get_link_flows", "tapgpu_get_trace", "tapgpu_set_capacity",
     "tapgpu_solve_scenarios", "tapgpu_sssp", "tapgpu_aon", "tapgpu_stream",
-    "tapgpu_profile_iteration", "tapgpu_run_iterations",
+    "tapgpu_profile_iteration", "tapgpu_run_iterations", "tapgpu_set_timing",
+    "tapgpu_get_timing",
 ]
 EXPORTED_DATA = ["num_cores", "num_threads", "using_fermi_architecture"]
 
@@ -122,10 +123,13 @@ def load(path: str | None = None):
     L.tapgpu_stream.restype = vp
     L.tapgpu_profile_iteration.argtypes = [vp, C.c_int, C.POINTER(C.c_float)]
     L.tapgpu_run_iterations.argtypes = [vp, C.c_int]
+    L.tapgpu_set_timing.argtypes = [vp, C.c_int]
+    L.tapgpu_get_timing.argtypes = [vp, F64P, I64P, I64P]
     for fn in ("tapgpu_create", "tapgpu_solve", "tapgpu_solve_begin", "tapgpu_solve_advance",
                "tapgpu_get_link_flows", "tapgpu_get_trace", "tapgpu_set_capacity",
                "tapgpu_solve_scenarios", "tapgpu_sssp", "tapgpu_aon",
-               "tapgpu_profile_iteration", "tapgpu_run_iterations"):
+               "tapgpu_profile_iteration", "tapgpu_run_iterations", "tapgpu_set_timing",
+               "tapgpu_get_timing"):
         getattr(L, fn).restype = C.c_int
     _LIB = L
     return L

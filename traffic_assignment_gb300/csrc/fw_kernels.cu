@@ -24,6 +24,9 @@
 
 #include <cfloat>
 #include <cstdio>
+#include <mutex>
+#include <set>
+#include <utility>
 
 namespace tapgpu {
 
@@ -679,10 +682,14 @@ __global__ void __launch_bounds__(kLinkBlock) k_step(LinkArgs a) {
 // that launches inside a stream capture never change function attributes.
 template <typename Fn>
 cudaError_t allow_max_smem(Fn fn) {
-  static bool done = false;
-  if (done) return cudaSuccess;
+  // one flag per kernel (all path kernels share the same function type)
+  static std::mutex mu;
+  static std::set<std::pair<const void*, int>> done_set;
   int dev = 0;
   cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  const auto key = std::make_pair(reinterpret_cast<const void*>(fn), dev);
+  if (done_set.count(key)) return cudaSuccess;
   cudaFuncAttributes fa;
   cudaError_t e = cudaFuncGetAttributes(&fa, fn);
   if (e != cudaSuccess) return e;
@@ -690,7 +697,7 @@ cudaError_t allow_max_smem(Fn fn) {
   const int dyn = max_smem_optin(dev) - static_cast<int>(fa.sharedSizeBytes);
   e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
   if (e == cudaSuccess)
-    done = true;
+    done_set.insert(key);
   else
     cudaGetLastError();
   return e;

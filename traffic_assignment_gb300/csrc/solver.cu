@@ -38,6 +38,7 @@ void set_message(const std::string& m) { g_message = m; }
 
 Ctx::~Ctx() {
   if (gexec) cudaGraphExecDestroy(gexec);
+  for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
   if (stream) cudaStreamDestroy(stream);
   for (auto& m : owned) cudaFree(m.p);
 }
@@ -54,6 +55,47 @@ int Ctx::alloc(void** p, size_t bytes) {
   }
   owned.push_back({q, bytes});
   *p = q;
+  return TAPGPU_OK;
+}
+
+cudaEvent_t Ctx::next_event() {
+  if (ev_used == ev_pool.size()) {
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    ev_pool.push_back(e);
+  }
+  return ev_pool[ev_used++];
+}
+
+// Record a timing event before (begin) or after a launch; inside a stream
+// capture the record becomes an event node of the graph.
+int Ctx::mark(int kind, bool begin) {
+  if (!timing) return TAPGPU_OK;
+  cudaEvent_t e = next_event();
+  if (!e) return TAPGPU_ERR_CUDA;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  TG_CUDA(cudaStreamIsCapturing(stream, &cs));
+  if (cs == cudaStreamCaptureStatusActive)
+    TG_CUDA(cudaEventRecordWithFlags(e, stream, cudaEventRecordExternal));
+  else
+    TG_CUDA(cudaEventRecord(e, stream));
+  if (begin)
+    timed.push_back({kind, e, nullptr});
+  else if (!timed.empty())
+    timed.back().b = e;
+  return TAPGPU_OK;
+}
+
+// Accumulate the durations of the marked launches (stream already synchronised).
+int Ctx::collect_timing() {
+  for (const Timed& t : timed) {
+    float ms = 0.f;
+    if (t.a && t.b && cudaEventElapsedTime(&ms, t.a, t.b) == cudaSuccess) {
+      kt_ms[t.kind] += ms;
+      kt_n[t.kind] += 1;
+    }
+  }
+  cudaGetLastError();
   return TAPGPU_OK;
 }
 
@@ -212,8 +254,8 @@ int Ctx::plan_launches() {
   aon_block = opt.aon_block > 0 ? opt.aon_block : 512;
   // leave room for the kernels' static shared memory (a few words)
   const size_t room = optin > 1024 ? static_cast<size_t>(optin - 1024) : 0;
-  sssp_smem = sssp_smem_bytes(n1, fp64) <= room;
-  aon_smem = aon_smem_bytes(n1) <= room;
+  sssp_smem = sssp_smem_bytes(n1, fp64) <= room && !opt.global_scratch;
+  aon_smem = aon_smem_bytes(n1) <= room && !opt.global_scratch;
   int so = sssp_occupancy(fp64, sssp_block, sssp_smem, n1);
   int ao = aon_occupancy(fp64, aon_block, aon_smem, n1);
   if (so <= 0 || ao <= 0) {
@@ -253,23 +295,45 @@ int Ctx::enqueue_paths(int nscen, bool load, const float* w32p, const double* w6
     a.scratch_stride = static_cast<long long>(sssp_smem_bytes(n1, fp64));
     TG_CUDA(cudaMemsetAsync(counters, 0, 2 * sizeof(int), stream));
     a.counter = counters;
+    if (measuring) TG_TRY(mark(0, true));
     TG_CUDA(launch_sssp(a, fp64, std::min(sssp_grid, ntask), sssp_block, sssp_smem, stream));
+    if (measuring) TG_TRY(mark(0, false));
     a.counter = counters + 1;
     a.scratch_stride = static_cast<long long>(aon_smem_bytes(n1));
+    if (measuring) TG_TRY(mark(1, true));
     TG_CUDA(launch_aon(a, fp64, std::min(aon_grid, ntask), aon_block, aon_smem, stream));
+    if (measuring) TG_TRY(mark(1, false));
+    count_launches(2);
   }
   return TAPGPU_OK;
 }
 
+void Ctx::count_launches(long long n) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(stream, &cs);
+  if (cs == cudaStreamCaptureStatusActive)
+    g_kernels += n;
+  else
+    launches += n;
+}
+
 int Ctx::enqueue_iteration(int nscen) {
-  TG_TRY(enqueue_paths(nscen, true, w32, w64, yfx, true));
+  measuring = true;
+  int rc = enqueue_paths(nscen, true, w32, w64, yfx, true);
+  measuring = false;
+  TG_TRY(rc);
   LinkArgs la = link_args(nscen);
+  TG_TRY(mark(2, true));
   for (int p = 0; p < kLsPasses; ++p) {
     la.pass = p;
     TG_CUDA(launch_ls_pass(la, link_grid, stream));
   }
   TG_CUDA(launch_ls_fallback(la, stream));
+  TG_TRY(mark(2, false));
+  TG_TRY(mark(3, true));
   TG_CUDA(launch_step(la, link_grid, stream));
+  TG_TRY(mark(3, false));
+  count_launches(kLsPasses + 2);
   return TAPGPU_OK;
 }
 
@@ -278,18 +342,26 @@ int Ctx::enqueue_initial(int nscen, bool warm) {
   LinkArgs la = link_args(nscen);
   if (!warm) {
     TG_CUDA(launch_set_costs(la, link_grid, stream));
+    count_launches(1);
     TG_TRY(enqueue_paths(nscen, true, w32, w64, yfx, true));
     la.pass = 0;
   } else {
     la.pass = 1;
   }
   TG_CUDA(launch_init_flows(la, link_grid, stream));
+  count_launches(1);
   return TAPGPU_OK;
 }
 
 int Ctx::run_graph(int iters, int nscen) {
   if (!opt.use_graphs) {
+    timed.clear();
+    ev_used = 0;
     for (int i = 0; i < iters; ++i) TG_TRY(enqueue_iteration(nscen));
+    if (timing) {
+      TG_CUDA(cudaStreamSynchronize(stream));
+      collect_timing();
+    }
     return TAPGPU_OK;
   }
   if (!gexec || g_iters != iters || g_nscen != nscen) {
@@ -297,6 +369,9 @@ int Ctx::run_graph(int iters, int nscen) {
       cudaGraphExecDestroy(gexec);
       gexec = nullptr;
     }
+    timed.clear();
+    ev_used = 0;
+    g_kernels = 0;
     cudaGraph_t graph = nullptr;
     TG_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     int rc = TAPGPU_OK;
@@ -321,6 +396,12 @@ int Ctx::run_graph(int iters, int nscen) {
     g_nscen = nscen;
   }
   TG_CUDA(cudaGraphLaunch(gexec, stream));
+  launches += g_kernels;
+  if (timing) {
+    // the graph's event nodes are re-recorded by every replay: read them now
+    TG_CUDA(cudaStreamSynchronize(stream));
+    collect_timing();
+  }
   return TAPGPU_OK;
 }
 
@@ -371,8 +452,10 @@ static int validate(const tapgpu_network* net, const tapgpu_demand* dem) {
   }
   for (int64_t k = 0; k < net->num_links; ++k) {
     const int64_t a = net->init[k], b = net->term[k];
-    if (a < 1 || a > net->num_nodes || b < 1 || b > net->num_nodes) {
-      set_message("link " + std::to_string(k) + " has a node outside 1..N");
+    // node 0 is the reference's unused row; 0-based graphs (the Python
+    // extension's) use it as an ordinary node
+    if (a < 0 || a > net->num_nodes || b < 0 || b > net->num_nodes) {
+      set_message("link " + std::to_string(k) + " has a node outside 0..N");
       return TAPGPU_ERR_ARG;
     }
     if (!(net->fft[k] >= 0) || !std::isfinite(net->fft[k]) || !(net->alpha[k] >= 0) ||
@@ -711,6 +794,7 @@ int tapgpu_solve_begin(tapgpu_ctx* ctx, int max_iters, double target_relgap, con
   TG_TRY(c->enqueue_initial(1, x0 != nullptr));
   TG_TRY(c->sync_check());
   c->solve_max_iters = max_iters;
+  c->last_nscen = 1;
   return TAPGPU_OK;
 }
 
@@ -803,6 +887,7 @@ int tapgpu_solve_scenarios(tapgpu_ctx* ctx, int num_scen, const int64_t* scen_pt
   }
   TG_CUDA(cudaSetDevice(c->device));
   TG_TRY(c->ensure_scenarios(num_scen));
+  c->last_nscen = num_scen;
   // capacities of every scenario: base with the scenario's edits
   std::vector<double> caps(static_cast<size_t>(num_scen) * M);
   for (int s = 0; s < num_scen; ++s) {
@@ -1003,20 +1088,62 @@ int tapgpu_run_iterations(tapgpu_ctx* ctx, int iters) {
   if (!ctx || iters < 1) return TAPGPU_ERR_ARG;
   Ctx* c = ctx->c;
   TG_CUDA(cudaSetDevice(c->device));
+  const int S = c->last_nscen;
   std::vector<tapgpu::ScenState> st;
-  TG_TRY(c->read_states(1, st));
-  st[0].done = 0;
-  st[0].max_iters = st[0].iter + iters;
-  st[0].target_relgap = 0.0;
-  TG_CUDA(cudaMemcpyAsync(c->state, st.data(), sizeof(tapgpu::ScenState), cudaMemcpyHostToDevice,
-                          c->stream));
-  std::vector<int> one{0};
-  if (c->h_scen_list != one) {
-    TG_CUDA(cudaMemcpyAsync(c->scen_list, one.data(), sizeof(int), cudaMemcpyHostToDevice,
-                            c->stream));
-    c->h_scen_list = one;
+  TG_TRY(c->read_states(S, st));
+  for (auto& s : st) {
+    s.done = 0;
+    s.max_iters = s.iter + iters;
+    s.target_relgap = 0.0;
   }
-  TG_TRY(c->run_graph(iters, 1));
+  TG_CUDA(cudaMemcpyAsync(c->state, st.data(), sizeof(tapgpu::ScenState) * S,
+                          cudaMemcpyHostToDevice, c->stream));
+  std::vector<int> all(S);
+  std::iota(all.begin(), all.end(), 0);
+  if (c->h_scen_list != all) {
+    TG_CUDA(cudaMemcpyAsync(c->scen_list, all.data(), sizeof(int) * S, cudaMemcpyHostToDevice,
+                            c->stream));
+    c->h_scen_list = all;
+  }
+  int per = c->opt.iters_per_launch > 0 ? c->opt.iters_per_launch : 8;
+  for (int done = 0; done < iters;) {
+    const int n = std::min(per, iters - done);
+    TG_TRY(c->run_graph(n, S));
+    done += n;
+  }
+  return TAPGPU_OK;
+}
+
+int tapgpu_set_timing(tapgpu_ctx* ctx, int on) {
+  if (!ctx) return TAPGPU_ERR_ARG;
+  Ctx* c = ctx->c;
+  TG_CUDA(cudaSetDevice(c->device));
+  TG_CUDA(cudaStreamSynchronize(c->stream));
+  if (c->gexec) {
+    cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+  }
+  c->timing = on != 0;
+  c->timed.clear();
+  c->ev_used = 0;
+  for (int i = 0; i < 4; ++i) {
+    c->kt_ms[i] = 0.0;
+    c->kt_n[i] = 0;
+  }
+  c->launches = 0;
+  return TAPGPU_OK;
+}
+
+int tapgpu_get_timing(tapgpu_ctx* ctx, double* ms, int64_t* counts, int64_t* kernel_launches) {
+  if (!ctx) return TAPGPU_ERR_ARG;
+  Ctx* c = ctx->c;
+  TG_CUDA(cudaSetDevice(c->device));
+  TG_CUDA(cudaStreamSynchronize(c->stream));
+  for (int i = 0; i < 4; ++i) {
+    if (ms) ms[i] = c->kt_ms[i];
+    if (counts) counts[i] = c->kt_n[i];
+  }
+  if (kernel_launches) *kernel_launches = c->launches;
   return TAPGPU_OK;
 }
 

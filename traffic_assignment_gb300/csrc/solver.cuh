@@ -76,6 +76,27 @@ struct Ctx {
   cudaGraphExec_t gexec = nullptr;
   int g_iters = 0, g_nscen = -1;
   int solve_max_iters = 0;
+  int last_nscen = 1;  // scenarios of the last solve (for run_iterations)
+
+  // kernel timing: event pairs recorded around launches (also inside graphs)
+  struct Timed {
+    int kind;  // 0 shortest paths, 1 loading, 2 line search, 3 step
+    cudaEvent_t a, b;
+  };
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  std::vector<Timed> timed;       // launches of the current graph (or direct enqueue)
+  double kt_ms[4] = {0, 0, 0, 0};
+  long long kt_n[4] = {0, 0, 0, 0};
+  long long launches = 0;         // kernels launched by the solver
+  long long g_kernels = 0;        // kernels in the current graph
+  long long pending_kernels = 0;  // kernels enqueued directly since the last sync
+  bool measuring = false;         // marks enabled for the path kernels of an iteration
+  cudaEvent_t next_event();
+  int mark(int kind, bool begin);
+  int collect_timing();
+  void count_launches(long long n);
 
   // launch shapes
   int sssp_block = 256, aon_block = 512, link_grid = 0;

@@ -56,7 +56,8 @@ class Solver:
     def __init__(self, net: Network, dem: Optional[Demand] = None, precision: str = "fp64",
                  device: int = 0, sssp_block: int = 0, aon_block: int = 0,
                  iters_per_launch: int = 0, use_graphs: bool = True, chunk_tasks: int = 0,
-                 record_tape: bool = False, tape_capacity: int = 0):
+                 record_tape: bool = False, tape_capacity: int = 0,
+                 global_scratch: bool = False):
         self.L = K.load()
         self.net = net
         self.dem = dem
@@ -71,6 +72,7 @@ class Solver:
         opt.chunk_tasks = chunk_tasks
         opt.record_tape = 1 if record_tape else 0
         opt.tape_capacity = tape_capacity
+        opt.global_scratch = 1 if global_scratch else 0
         self.precision = "fp32" if opt.precision == K.TAPGPU_FP32_PATHS else "fp64"
         keep: list = []
         ns = _net_struct(net, keep)
@@ -178,6 +180,22 @@ class Solver:
 
     def run_iterations(self, iters: int):
         K.check(self.L.tapgpu_run_iterations(self.h, int(iters)))
+
+    def set_timing(self, on: bool = True):
+        K.check(self.L.tapgpu_set_timing(self.h, 1 if on else 0))
+
+    def timing(self) -> Dict[str, float]:
+        """Accumulated kernel times (ms) and launch counts since set_timing()."""
+        ms = np.zeros(4)
+        n = np.zeros(4, np.int64)
+        kl = np.zeros(1, np.int64)
+        K.check(self.L.tapgpu_get_timing(self.h, K.ptr(ms, K.F64P), K.ptr(n, K.I64P),
+                                         K.ptr(kl, K.I64P)))
+        names = ("sssp", "aon", "line_search", "step")
+        out = {f"{k}_ms": float(ms[i]) for i, k in enumerate(names)}
+        out.update({f"{k}_launches": int(n[i]) for i, k in enumerate(names)})
+        out["kernel_launches"] = int(kl[0])
+        return out
 
     def profile_iteration(self, reps: int = 5) -> Dict[str, float]:
         ms = (C.c_float * 5)()

@@ -388,6 +388,12 @@ def make_grid10k(seed: int = 1003):
     return _arterial_grid(seed, 100, 200, 1000, 1.5e6, 25.0)
 
 
+def make_grid3600(seed: int = 1007):
+    """60 x 60 grid + 40 arterials, 100 zones: a mid-size test network whose
+    per-origin shared-memory working set exceeds the 48 KB default."""
+    return _arterial_grid(seed, 60, 40, 100, 1.5e5, 15.0)
+
+
 def make_grid100k(seed: int = 1005, num_zones: int = 4000):
     """316 x 316 grid + arterials: 99,856 nodes, ~400,000 links, 4,000 zones."""
     return _arterial_grid(seed, 316, 2000, num_zones, 15.0e6, 60.0)
@@ -429,6 +435,7 @@ def make_workload(name: str, seed: Optional[int] = None):
     table = {
         "small24": make_small24,
         "grid416": make_grid416,
+        "grid3600": make_grid3600,
         "grid10k": make_grid10k,
         "grid100k": make_grid100k,
     }
