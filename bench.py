@@ -347,6 +347,23 @@ def run_ours(args, rank, world, local_rank):
     return 0
 
 
+def profile_case(kind):
+    """A few FW iterations on the 10k-node network: every kernel of the loop
+    launches a handful of times (1,000 or 16,000 shortest-path tasks each)."""
+    from traffic_assignment_gb300 import Solver, synth
+    net, dem = synth.make_grid10k()
+    with Solver(net, dem, precision="fp32") as s:
+        r = s.solve(max_iters=4)
+        if kind == "batched":
+            x0, _ = s.flows()
+            s.solve_scenarios(synth.make_scenarios(net, 16), max_iters=3, x0=x0)
+        s.set_timing(True)
+        s.run_iterations(2)
+        tm = s.timing()
+    print(json.dumps({"profile_case": kind, "iterations": r["iterations"], **tm}))
+    return 0
+
+
 def solver_chunk_tasks(solver, tasks):
     """Tasks per shortest-path launch (the label buffer holds 2 GiB by default)."""
     per_task = (solver.n1) * (4 if solver.precision == "fp32" else 8)
@@ -366,8 +383,13 @@ def main():
     ap.add_argument("--plain-scenarios", type=int, default=8)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-case", choices=["plain", "batched"], default=None,
+                    help="small case for ncu: a few FW iterations of the 10k-node network, "
+                         "one scenario (plain) or 16 scenarios (batched), then exit")
     args = ap.parse_args()
     rank, world, local_rank = _env_rank()
+    if args.profile_case:
+        return profile_case(args.profile_case)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -316,6 +316,9 @@ int tapgpu_run_iterations(tapgpu_ctx *ctx, int iters);
  * the solver launched since the reset. */
 int tapgpu_set_timing(tapgpu_ctx *ctx, int on);
 int tapgpu_get_timing(tapgpu_ctx *ctx, double *ms, int64_t *counts, int64_t *kernel_launches);
+/* Shortest-path work counters gathered while timing is on: out[0] label
+ * correction rounds, out[1] (scenario, origin) tasks, out[2] node expansions. */
+int tapgpu_get_path_stats(tapgpu_ctx *ctx, int64_t *out);
 
 #ifdef __cplusplus
 }

@@ -49,7 +49,9 @@ def build_oracle(force: bool = False) -> str:
     srcs = [os.path.join(HERE, "oracle_tap.c"), os.path.join(HERE, "oracle_tap.h")]
     if force or _stale(out, srcs):
         tmp = out + ".tmp"
-        _run(["gcc", *CFLAGS, "-std=c11", "-fPIC", "-shared", "-o", tmp, srcs[0], "-lm"])
+        # no fused multiply-add: the Arm host would otherwise round differently
+        _run(["gcc", *CFLAGS, "-ffp-contract=off", "-std=c11", "-fPIC", "-shared", "-o", tmp,
+              srcs[0], "-lm"])
         os.replace(tmp, out)
     return out
 

@@ -78,7 +78,7 @@ EXPORTED = [
     "tapgpu_get_link_flows", "tapgpu_get_trace", "tapgpu_set_capacity",
     "tapgpu_solve_scenarios", "tapgpu_sssp", "tapgpu_aon", "tapgpu_stream",
     "tapgpu_profile_iteration", "tapgpu_run_iterations", "tapgpu_set_timing",
-    "tapgpu_get_timing",
+    "tapgpu_get_timing", "tapgpu_get_path_stats",
 ]
 EXPORTED_DATA = ["num_cores", "num_threads", "using_fermi_architecture"]
 
@@ -125,6 +125,8 @@ def load(path: str | None = None):
     L.tapgpu_run_iterations.argtypes = [vp, C.c_int]
     L.tapgpu_set_timing.argtypes = [vp, C.c_int]
     L.tapgpu_get_timing.argtypes = [vp, F64P, I64P, I64P]
+    L.tapgpu_get_path_stats.argtypes = [vp, I64P]
+    L.tapgpu_get_path_stats.restype = C.c_int
     for fn in ("tapgpu_create", "tapgpu_solve", "tapgpu_solve_begin", "tapgpu_solve_advance",
                "tapgpu_get_link_flows", "tapgpu_get_trace", "tapgpu_set_capacity",
                "tapgpu_solve_scenarios", "tapgpu_sssp", "tapgpu_aon",

@@ -80,35 +80,74 @@ __device__ __forceinline__ int nth_set_bit(unsigned w, int n) {
   return pos;
 }
 
+// Edge records of one scenario.  FP32 paths read one packed 8-byte record
+// {head, weight bits} per edge; FP64 paths read head and weight separately.
 template <typename T>
-__device__ __forceinline__ const T* weights_of(const PathArgs& a, int scen);
+struct Edges;
 template <>
-__device__ __forceinline__ const float* weights_of<float>(const PathArgs& a, int scen) {
-  return a.w32 + static_cast<size_t>(scen) * a.g.m;
+struct Edges<float> {
+  const uint2* e;
+  __device__ __forceinline__ void load(int i, int& h, float& w) const {
+    const uint2 r = __ldg(e + i);
+    h = static_cast<int>(r.x);
+    w = __uint_as_float(r.y);
+  }
+  __device__ __forceinline__ float weight(int i) const { return __uint_as_float(__ldg(&e[i].y)); }
+};
+template <>
+struct Edges<double> {
+  const int* head;
+  const double* w;
+  __device__ __forceinline__ void load(int i, int& h, double& x) const {
+    h = __ldg(head + i);
+    x = __ldg(w + i);
+  }
+  __device__ __forceinline__ double weight(int i) const { return __ldg(w + i); }
+};
+
+template <typename T>
+__device__ __forceinline__ Edges<T> edges_of(const PathArgs& a, int scen);
+template <>
+__device__ __forceinline__ Edges<float> edges_of<float>(const PathArgs& a, int scen) {
+  return Edges<float>{a.e32 + static_cast<size_t>(scen) * a.g.m};
 }
 template <>
-__device__ __forceinline__ const double* weights_of<double>(const PathArgs& a, int scen) {
-  return a.w64 + static_cast<size_t>(scen) * a.g.m;
+__device__ __forceinline__ Edges<double> edges_of<double>(const PathArgs& a, int scen) {
+  return Edges<double>{a.g.head, a.w64 + static_cast<size_t>(scen) * a.g.m};
 }
 
-// Relax the out-links of v; returns 1 if any head label dropped.
+constexpr int kEdgeGroup = 4;  // edge records fetched together before relaxing
+
+// Relax the out-links of v; returns 1 if any head label dropped.  The edge
+// records of a group are all requested before the first atomic so that
+// their memory latencies overlap.
 template <typename T>
-__device__ __forceinline__ int relax_node(int v, int src, const Graph& g, const T* __restrict__ wt,
+__device__ __forceinline__ int relax_node(int v, int src, const Graph& g, const Edges<T>& ed,
                                           typename DT<T>::U* dist, unsigned* nxt) {
   using U = typename DT<T>::U;
   if (v < g.first_thru && v != src) return 0;  // zones are never passed through
-  const T du = DT<T>::val(vload(dist + v));
+  const int e0 = __ldg(g.row_ptr + v);
   const int e1 = __ldg(g.row_ptr + v + 1);
+  const T du = DT<T>::val(vload(dist + v));
   int pushed = 0;
-  for (int e = __ldg(g.row_ptr + v); e < e1; ++e) {
-    const int h = __ldg(g.head + e);
-    const U nb = DT<T>::bits(DT<T>::add(du, __ldg(wt + e)));
-    if (nb < vload(dist + h)) {
-      const U old = atomicMin(dist + h, nb);
-      if (nb < old) {
-        const unsigned bit = 1u << (h & 31);
-        if (!(vload(nxt + (h >> 5)) & bit)) atomicOr(nxt + (h >> 5), bit);
-        pushed = 1;
+  for (int b = e0; b < e1; b += kEdgeGroup) {
+    int hh[kEdgeGroup];
+    T ww[kEdgeGroup];
+#pragma unroll
+    for (int j = 0; j < kEdgeGroup; ++j)
+      if (b + j < e1) ed.load(b + j, hh[j], ww[j]);
+#pragma unroll
+    for (int j = 0; j < kEdgeGroup; ++j) {
+      if (b + j >= e1) break;
+      const int h = hh[j];
+      const U nb = DT<T>::bits(DT<T>::add(du, ww[j]));
+      if (nb < vload(dist + h)) {
+        const U old = atomicMin(dist + h, nb);
+        if (nb < old) {
+          const unsigned bit = 1u << (h & 31);
+          if (!(vload(nxt + (h >> 5)) & bit)) atomicOr(nxt + (h >> 5), bit);
+          pushed = 1;
+        }
       }
     }
   }
@@ -142,7 +181,8 @@ __global__ void __launch_bounds__(BLOCK) k_sssp(PathArgs a) {
     const int scen = a.scen_list ? a.scen_list[slot] : 0;
     if (a.state && a.state[scen].done) continue;
     const int src = a.sources[task - slot * a.num_sources];
-    const T* wt = weights_of<T>(a, scen);
+    const Edges<T> ed = edges_of<T>(a, scen);
+    unsigned expanded = 0;
 
     for (int v = threadIdx.x; v < n1; v += BLOCK) dist[v] = DT<T>::kInf;
     for (int i = threadIdx.x; i < 2 * nwords; i += BLOCK) bm0[i] = 0u;
@@ -188,7 +228,8 @@ __global__ void __launch_bounds__(BLOCK) k_sssp(PathArgs a) {
           if (j < total) {
             const int rank = j - (oincl - __popc(ow));
             const int v = (((c << 5) + owner) << 5) + nth_set_bit(ow, rank);
-            pushed |= relax_node<T>(v, src, a.g, wt, dist, nxt);
+            pushed |= relax_node<T>(v, src, a.g, ed, dist, nxt);
+            ++expanded;
           }
         }
       }
@@ -204,6 +245,14 @@ __global__ void __launch_bounds__(BLOCK) k_sssp(PathArgs a) {
     }
     T* out = static_cast<T*>(a.dist) + static_cast<size_t>(task - a.task_begin) * n1;
     for (int v = threadIdx.x; v < n1; v += BLOCK) out[v] = DT<T>::val(dist[v]);
+    if (a.stats) {  // rounds and node expansions of this task
+      for (int o = 16; o >= 1; o >>= 1) expanded += __shfl_down_sync(kFull, expanded, o);
+      if (lane == 0) atomicAdd(a.stats + 2, static_cast<unsigned long long>(expanded));
+      if (threadIdx.x == 0) {
+        atomicAdd(a.stats + 0, static_cast<unsigned long long>(rounds));
+        atomicAdd(a.stats + 1, 1ull);
+      }
+    }
   }
 }
 
@@ -232,7 +281,7 @@ __global__ void __launch_bounds__(BLOCK) k_aon(PathArgs a) {
     if (a.state && a.state[scen].done) continue;
     const int sidx = task - slot * a.num_sources;
     const int src = a.sources[sidx];
-    const T* wt = weights_of<T>(a, scen);
+    const Edges<T> ed = edges_of<T>(a, scen);
     const T* din = static_cast<const T*>(a.dist) + static_cast<size_t>(task - a.task_begin) * n1;
 
     for (int v = threadIdx.x; v < n1; v += BLOCK) dS[v] = din[v];
@@ -251,7 +300,7 @@ __global__ void __launch_bounds__(BLOCK) k_aon(PathArgs a) {
           const int u = __ldg(a.g.tail + k);
           if (u < F && u != src) continue;
           const T du = dS[u];
-          if (du < dv && DT<T>::add(du, __ldg(wt + k)) == dv) {
+          if (du < dv && DT<T>::add(du, ed.weight(k)) == dv) {
             p = k;
             break;
           }
@@ -276,7 +325,7 @@ __global__ void __launch_bounds__(BLOCK) k_aon(PathArgs a) {
           const int u = __ldg(a.g.tail + k);
           if (u < F && u != src) continue;
           if (!(u == src || pred[u] >= 0)) continue;
-          if (DT<T>::add(dS[u], __ldg(wt + k)) == dv) {
+          if (DT<T>::add(dS[u], ed.weight(k)) == dv) {
             c = k;
             break;
           }
@@ -431,8 +480,11 @@ __device__ __forceinline__ bool last_block(unsigned* arrive) {
   return sh_ticket == gridDim.x - 1;
 }
 
-__device__ __forceinline__ void write_weights(const LinkArgs& a, size_t i, double t) {
-  if (a.w32) a.w32[i] = __double2float_rn(t);
+// shortest-path weight of link k of the scenario at offset i - k
+__device__ __forceinline__ void write_weights(const LinkArgs& a, size_t i, int k, double t) {
+  if (a.e32)
+    a.e32[i] = make_uint2(static_cast<unsigned>(__ldg(a.head + k)),
+                          __float_as_uint(__double2float_rn(t)));
   if (a.w64) a.w64[i] = t;
 }
 
@@ -457,7 +509,7 @@ __global__ void __launch_bounds__(kLinkBlock) k_init_flows(LinkArgs a, int from_
     a.t[off + k] = t;
     if (a.dtdx)
       a.dtdx[off + k] = bpr_dq(a.lp.fft[k], a.lp.alpha[k], a.lp.beta[k], a.lp.ipow[k], cap[k], x);
-    write_weights(a, off + k, t);
+    write_weights(a, off + k, k, t);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     ScenState& st = a.state[scen];
@@ -483,7 +535,7 @@ __global__ void __launch_bounds__(kLinkBlock) k_set_free_flow(LinkArgs a) {
   const size_t off = static_cast<size_t>(scen) * a.m;
   for (int k = blockIdx.x * kLinkBlock + threadIdx.x; k < a.m; k += gridDim.x * kLinkBlock) {
     a.y_fx[off + k] = 0ull;
-    write_weights(a, off + k, a.lp.fft[k]);
+    write_weights(a, off + k, k, a.lp.fft[k]);
   }
 }
 
@@ -646,7 +698,7 @@ __global__ void __launch_bounds__(kLinkBlock) k_step(LinkArgs a) {
     const double t = bpr(fft, al, be, ip, c, x);
     a.t[off + k] = t;
     if (a.dtdx) a.dtdx[off + k] = bpr_dq(fft, al, be, ip, c, x);
-    write_weights(a, off + k, t);
+    write_weights(a, off + k, k, t);
     acc[0] = __dadd_rn(acc[0], __dmul_rn(x, t));
   }
   block_sum<1, kLinkBlock>(acc, sh);

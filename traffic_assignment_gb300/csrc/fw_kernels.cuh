@@ -69,7 +69,7 @@ struct Demand {
 
 struct PathArgs {
   Graph g;
-  const float* w32;             // [S][m] when fp32 paths
+  const uint2* e32;             // [S][m] {head, f32 weight bits} when fp32 paths
   const double* w64;            // [S][m] when fp64 paths
   const int* sources;           // source nodes
   int num_sources;
@@ -89,6 +89,7 @@ struct PathArgs {
   int do_load;                  // 0: predecessors only
   void* scratch;                // per-CTA global scratch when the smem variant does not fit
   long long scratch_stride;     // bytes per CTA
+  unsigned long long* stats;    // optional [4]: rounds, tasks, node expansions, -
 };
 
 struct LinkArgs {
@@ -101,7 +102,8 @@ struct LinkArgs {
   double* t;                    // [S][m]
   double* d;                    // [S][m]
   unsigned long long* y_fx;     // [S][m]
-  float* w32;                   // [S][m] or nullptr
+  uint2* e32;                   // [S][m] packed fp32 edge records, or nullptr
+  const int* head;              // [m] head node of each link (for e32)
   double* w64;                  // [S][m] or nullptr
   double* dtdx;                 // [S][m] or nullptr (derivative of the BPR cost)
   double* partials;             // [S][gridDim.x][kNumSums]

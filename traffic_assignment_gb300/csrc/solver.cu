@@ -163,6 +163,7 @@ PathArgs Ctx::path_args(int nscen_slots) const {
   a.do_load = 1;
   a.scratch = path_scratch;
   a.scratch_stride = 0;
+  a.stats = timing ? path_stats : nullptr;
   return a;
 }
 
@@ -178,7 +179,8 @@ LinkArgs Ctx::link_args(int nscen) const {
   a.t = t;
   a.d = d;
   a.y_fx = yfx;
-  a.w32 = fp64 ? nullptr : w32;
+  a.e32 = fp64 ? nullptr : e32;
+  a.head = head;
   a.w64 = fp64 ? w64 : nullptr;
   a.dtdx = dtdx;
   a.partials = partials;
@@ -199,12 +201,12 @@ LinkArgs Ctx::link_args(int nscen) const {
 int Ctx::ensure_scenarios(int S) {
   if (S <= S_cap) return TAPGPU_OK;
   // release the old per-scenario arrays
-  void* olds[] = {cap, x, t, d, dtdx, yfx, w32, w64, state, partials, arrive, trace, scen_list,
+  void* olds[] = {cap, x, t, d, dtdx, yfx, e32, w64, state, partials, arrive, trace, scen_list,
                   x_hist, d_hist, lam_hist};
   for (void* p : olds) free_owned(this, p);
   cap = x = t = d = dtdx = nullptr;
   yfx = nullptr;
-  w32 = nullptr;
+  e32 = nullptr;
   w64 = nullptr;
   state = nullptr;
   partials = nullptr;
@@ -221,7 +223,7 @@ int Ctx::ensure_scenarios(int S) {
   if (fp64)
     TG_TRY(alloc_n(&w64, sm));
   else
-    TG_TRY(alloc_n(&w32, sm));
+    TG_TRY(alloc_n(&e32, sm));
   if (opt.record_tape) TG_TRY(alloc_n(&dtdx, sm));
   TG_TRY(alloc_n(&state, static_cast<size_t>(S)));
   TG_TRY(alloc_n(&partials, static_cast<size_t>(S) * link_grid * kNumSums));
@@ -275,13 +277,13 @@ int Ctx::plan_launches() {
   return TAPGPU_OK;
 }
 
-int Ctx::enqueue_paths(int nscen, bool load, const float* w32p, const double* w64p,
+int Ctx::enqueue_paths(int nscen, bool load, const uint2* e32p, const double* w64p,
                        unsigned long long* ydst, bool use_state) {
   const int64_t tasks = static_cast<int64_t>(nscen) * Z;
   for (int64_t t0 = 0; t0 < tasks; t0 += dist_tasks) {
     const int64_t t1 = std::min(tasks, t0 + dist_tasks);
     PathArgs a = path_args(nscen);
-    a.w32 = w32p;
+    a.e32 = e32p;
     a.w64 = w64p;
     a.y_fx = ydst;
     a.do_load = load ? 1 : 0;
@@ -319,7 +321,7 @@ void Ctx::count_launches(long long n) {
 
 int Ctx::enqueue_iteration(int nscen) {
   measuring = true;
-  int rc = enqueue_paths(nscen, true, w32, w64, yfx, true);
+  int rc = enqueue_paths(nscen, true, e32, w64, yfx, true);
   measuring = false;
   TG_TRY(rc);
   LinkArgs la = link_args(nscen);
@@ -343,7 +345,7 @@ int Ctx::enqueue_initial(int nscen, bool warm) {
   if (!warm) {
     TG_CUDA(launch_set_costs(la, link_grid, stream));
     count_launches(1);
-    TG_TRY(enqueue_paths(nscen, true, w32, w64, yfx, true));
+    TG_TRY(enqueue_paths(nscen, true, e32, w64, yfx, true));
     la.pass = 0;
   } else {
     la.pass = 1;
@@ -631,7 +633,9 @@ static int create_impl(const tapgpu_network* net, const tapgpu_demand* dem,
   TG_TRY(c->alloc_n(&c->counters, 2));
   TG_TRY(c->alloc_n(&c->err, 1));
   TG_TRY(c->alloc_n(&c->err_info, 2));
+  TG_TRY(c->alloc_n(&c->path_stats, 4));
   TG_CUDA(cudaMemset(c->err, 0, sizeof(int)));
+  TG_CUDA(cudaMemset(c->path_stats, 0, 4 * sizeof(unsigned long long)));
 
   // shortest-path label scratch between the two path kernels
   const size_t tb = static_cast<size_t>(n1) * (c->fp64 ? 8 : 4);
@@ -640,7 +644,7 @@ static int create_impl(const tapgpu_network* net, const tapgpu_demand* dem,
   chunk = std::max<int64_t>(1, std::min<int64_t>(chunk, 1 << 30));
   c->dist_tasks = std::min<int64_t>(chunk, std::max<int64_t>(Z, 1) * 4096);
   TG_TRY(c->alloc(&c->dist, tb * c->dist_tasks));
-  TG_TRY(c->alloc_n(&c->api_w32, M));
+  TG_TRY(c->alloc_n(&c->api_e32, M));
   TG_TRY(c->alloc_n(&c->api_w64, M));
   TG_TRY(c->alloc_n(&c->api_yfx, M));
   TG_TRY(c->ensure_scenarios(1));
@@ -924,7 +928,7 @@ int tapgpu_solve_scenarios(tapgpu_ctx* ctx, int num_scen, const int64_t* scen_pt
     // once and start every scenario from it
     tapgpu::LinkArgs la = c->link_args(1);
     TG_CUDA(tapgpu::launch_set_costs(la, c->link_grid, c->stream));
-    TG_TRY(c->enqueue_paths(1, true, c->w32, c->w64, c->yfx, true));
+    TG_TRY(c->enqueue_paths(1, true, c->e32, c->w64, c->yfx, true));
     for (int s = 1; s < num_scen; ++s)
       TG_CUDA(cudaMemcpyAsync(c->yfx + static_cast<size_t>(s) * M, c->yfx,
                               sizeof(unsigned long long) * M, cudaMemcpyDeviceToDevice,
@@ -945,7 +949,7 @@ int tapgpu_solve_scenarios(tapgpu_ctx* ctx, int num_scen, const int64_t* scen_pt
 
 static int to_device_weights(Ctx* c, const double* weights) {
   std::vector<double> w(c->M);
-  std::vector<float> wf(c->M);
+  std::vector<uint2> wf(c->M);
   for (int k = 0; k < c->M; ++k) {
     const double v = weights[c->perm[k]];
     if (!(v >= 0) || std::isinf(v)) {
@@ -953,11 +957,14 @@ static int to_device_weights(Ctx* c, const double* weights) {
       return TAPGPU_ERR_ARG;
     }
     w[k] = v;
-    wf[k] = static_cast<float>(v);
+    const float f = static_cast<float>(v);
+    unsigned bits;
+    std::memcpy(&bits, &f, sizeof bits);
+    wf[k] = make_uint2(static_cast<unsigned>(c->h_head[k]), bits);
   }
   TG_CUDA(cudaMemcpyAsync(c->api_w64, w.data(), sizeof(double) * c->M, cudaMemcpyHostToDevice,
                           c->stream));
-  TG_CUDA(cudaMemcpyAsync(c->api_w32, wf.data(), sizeof(float) * c->M, cudaMemcpyHostToDevice,
+  TG_CUDA(cudaMemcpyAsync(c->api_e32, wf.data(), sizeof(uint2) * c->M, cudaMemcpyHostToDevice,
                           c->stream));
   TG_CUDA(cudaStreamSynchronize(c->stream));
   return TAPGPU_OK;
@@ -1003,7 +1010,7 @@ int tapgpu_sssp(tapgpu_ctx* ctx, const double* weights, const int64_t* srcs, int
     a.task_begin = 0;
     a.task_end = ns;
     a.w64 = c->api_w64;
-    a.w32 = nullptr;
+    a.e32 = nullptr;
     a.do_load = 0;
     a.pred_out = c->pred_buf;
     a.y_fx = c->api_yfx;
@@ -1071,7 +1078,7 @@ int tapgpu_aon(tapgpu_ctx* ctx, const double* weights, double* volume) {
   TG_TRY(to_device_weights(c, weights));
   TG_CUDA(cudaMemsetAsync(c->api_yfx, 0, sizeof(unsigned long long) * c->M, c->stream));
   TG_CUDA(cudaMemsetAsync(c->err, 0, sizeof(int), c->stream));
-  TG_TRY(c->enqueue_paths(1, true, c->fp64 ? nullptr : c->api_w32, c->fp64 ? c->api_w64 : nullptr,
+  TG_TRY(c->enqueue_paths(1, true, c->fp64 ? nullptr : c->api_e32, c->fp64 ? c->api_w64 : nullptr,
                           c->api_yfx, false));
   TG_TRY(c->sync_check());
   std::vector<unsigned long long> y(c->M);
@@ -1131,6 +1138,18 @@ int tapgpu_set_timing(tapgpu_ctx* ctx, int on) {
     c->kt_n[i] = 0;
   }
   c->launches = 0;
+  TG_CUDA(cudaMemset(c->path_stats, 0, 4 * sizeof(unsigned long long)));
+  return TAPGPU_OK;
+}
+
+int tapgpu_get_path_stats(tapgpu_ctx* ctx, int64_t* out) {
+  if (!ctx || !out) return TAPGPU_ERR_ARG;
+  Ctx* c = ctx->c;
+  TG_CUDA(cudaSetDevice(c->device));
+  TG_CUDA(cudaStreamSynchronize(c->stream));
+  unsigned long long v[4];
+  TG_CUDA(cudaMemcpy(v, c->path_stats, sizeof(v), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < 4; ++i) out[i] = static_cast<int64_t>(v[i]);
   return TAPGPU_OK;
 }
 
@@ -1173,7 +1192,7 @@ int tapgpu_profile_iteration(tapgpu_ctx* ctx, int reps, float* ms) {
     cudaMemsetAsync(c->counters, 0, 2 * sizeof(int), c->stream);
     a.counter = c->counters;
     a.scratch_stride = static_cast<long long>(tapgpu::sssp_smem_bytes(c->n1, c->fp64));
-    a.w32 = c->fp64 ? nullptr : c->w32;
+    a.e32 = c->fp64 ? nullptr : c->e32;
     a.w64 = c->fp64 ? c->w64 : nullptr;
     if (tasks > c->dist_tasks) {
       rc = TAPGPU_ERR_UNSUPPORTED;

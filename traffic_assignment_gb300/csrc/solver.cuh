@@ -46,7 +46,7 @@ struct Ctx {
   int S_cap = 0;
   double *cap = nullptr, *x = nullptr, *t = nullptr, *d = nullptr, *dtdx = nullptr;
   unsigned long long* yfx = nullptr;
-  float* w32 = nullptr;
+  uint2* e32 = nullptr;  // packed {head, f32 weight} per scenario and link
   double* w64 = nullptr;
   ScenState* state = nullptr;
   double* partials = nullptr;
@@ -67,8 +67,9 @@ struct Ctx {
   int* err = nullptr;       // [1]
   int* err_info = nullptr;  // [2]
   int* pred_buf = nullptr;  // [dist_tasks][n1] for the shortest-path API
+  unsigned long long* path_stats = nullptr;  // [4] rounds, tasks, expansions (timing on)
   // buffers of the one-shot API (weights in both precisions, loaded volumes)
-  float* api_w32 = nullptr;
+  uint2* api_e32 = nullptr;
   double* api_w64 = nullptr;
   unsigned long long* api_yfx = nullptr;
 
@@ -121,7 +122,7 @@ struct Ctx {
   LinkArgs link_args(int nscen) const;
 
   // enqueue helpers (stream ordered, capturable)
-  int enqueue_paths(int nscen, bool load, const float* w32p, const double* w64p,
+  int enqueue_paths(int nscen, bool load, const uint2* e32p, const double* w64p,
                     unsigned long long* ydst, bool use_state);
   int enqueue_iteration(int nscen);
   int enqueue_initial(int nscen, bool warm);
