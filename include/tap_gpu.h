@@ -236,6 +236,7 @@ typedef struct tapgpu_options_s {
   int record_tape;       /* keep per-iteration flows and directions for the adjoint */
   int tape_capacity;     /* iterations kept on the tape */
   int global_scratch;    /* 1: per-CTA labels in global memory even when shared memory fits */
+  int sssp_variant;      /* 0 default; 1 bulk-synchronous rounds; 2 asynchronous warp-owned frontier */
 } tapgpu_options;
 
 typedef struct tapgpu_result_s {

@@ -41,12 +41,16 @@ def test_aon_matches_oracle(built_lib, grid416):
             assert _rel(y, ref) < 1e-12
 
 
+VARIANTS = ["rounds", "async"]
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
 @pytest.mark.parametrize("name", ["small24", "grid416"])
-def test_fw_fp64_parity(built_lib, name):
+def test_fw_fp64_parity(built_lib, name, variant):
     net, dem = synth.make_workload(name)
     iters = 60
     ref = oracle.frankwolfe(net, dem, threads=1, max_iters=iters)
-    with Solver(net, dem, precision="fp64") as s:
+    with Solver(net, dem, precision="fp64", sssp_variant=variant) as s:
         r = s.solve(max_iters=iters)
         x, t = s.flows()
         tr = s.trace()
@@ -84,14 +88,15 @@ def test_relgap_stopping_rule(built_lib, grid416):
     assert r["relgap"] <= 1e-3
 
 
-def test_sssp_labels_bit_exact(built_lib, grid416):
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_sssp_labels_bit_exact(built_lib, grid416, variant):
     net, _ = grid416
     va, ea = net.csr()
     rng = np.random.default_rng(7)
     w = net.fft * rng.uniform(0.5, 2.0, net.num_links)
     srcs = np.arange(1, net.num_nodes + 1, 7)
     dref, _ = oracle.sssp_all(va, ea, w, net.num_nodes + 1, srcs, net.first_thru_node)
-    with Solver(net, None) as s:
+    with Solver(net, None, sssp_variant=variant) as s:
         d, p = s.sssp(w, srcs)
     np.testing.assert_array_equal(d, dref)
     # every predecessor path re-sums to its label (cuda_sssp/sssp.cu:155-250)
@@ -146,14 +151,16 @@ def test_warm_start(built_lib, grid416):
     assert abs(r["relgap"] - ref["relgap"]) <= RTOL64 * abs(ref["relgap"])
 
 
+@pytest.mark.parametrize("variant", VARIANTS)
 @pytest.mark.parametrize("precision,global_scratch",
                          [("fp64", False), ("fp32", False), ("fp64", True), ("fp32", True)])
-def test_medium_network_variants(built_lib, precision, global_scratch):
+def test_medium_network_variants(built_lib, precision, global_scratch, variant):
     """3,600 nodes: labels and trees no longer fit the 48 KB default (opt-in
     shared memory), and the global-memory scratch variant gives the same answer."""
     net, dem = synth.make_grid3600()
     ref = oracle.frankwolfe(net, dem, threads=4, max_iters=12)
-    with Solver(net, dem, precision=precision, global_scratch=global_scratch) as s:
+    with Solver(net, dem, precision=precision, global_scratch=global_scratch,
+                sssp_variant=variant) as s:
         r = s.solve(max_iters=12)
         x, _ = s.flows()
     assert r["error_bits"] == 0
@@ -181,3 +188,32 @@ def test_deterministic_fp32(built_lib, grid416):
             s.solve(max_iters=15)
             outs.append(s.flows()[0])
     np.testing.assert_array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_sssp_golden_graphs(built_lib, golden_dir, variant):
+    """The reference's own SSSP test graphs (rmat.txt.martin, okuyama example)
+    and an integer grid: labels equal sssp_pape_lll's (stored golden values)."""
+    import glob
+    import os
+    from traffic_assignment_gb300.synth import Network
+    for path in sorted(glob.glob(os.path.join(golden_dir, "sssp_*.npz"))):
+        z = np.load(path)
+        m = len(z["init"])
+        net = Network(num_nodes=int(z["num_nodes"]), num_zones=0,
+                      first_thru_node=int(z["first_thru_node"]), init=z["init"], term=z["term"],
+                      capacity=np.ones(m), length=np.ones(m), fft=np.zeros(m), alpha=np.zeros(m),
+                      beta=np.ones(m), speed=np.zeros(m), toll=np.zeros(m),
+                      link_type=np.ones(m, np.int16))
+        with Solver(net, None, sssp_variant=variant) as s:
+            d, p = s.sssp(z["weight"], z["sources"])
+        np.testing.assert_array_equal(d, z["dist"], err_msg=path)
+        # predecessors may differ on ties, but each must be a tight in-link
+        for i in range(len(z["sources"])):
+            for v in range(1, int(z["num_nodes"]) + 1):
+                k = p[i, v]
+                if k < 0:
+                    assert v == z["sources"][i] or d[i, v] == np.finfo(float).max
+                else:
+                    assert z["term"][k] == v
+                    assert d[i, z["init"][k]] + z["weight"][k] == d[i, v]

@@ -45,7 +45,8 @@ class Options(C.Structure):
     _fields_ = [("precision", C.c_int), ("device", C.c_int), ("sssp_block", C.c_int),
                 ("aon_block", C.c_int), ("iters_per_launch", C.c_int), ("use_graphs", C.c_int),
                 ("chunk_tasks", C.c_int64), ("record_tape", C.c_int),
-                ("tape_capacity", C.c_int), ("global_scratch", C.c_int)]
+                ("tape_capacity", C.c_int), ("global_scratch", C.c_int),
+                ("sssp_variant", C.c_int)]
 
 
 class Result(C.Structure):

@@ -256,6 +256,203 @@ __global__ void __launch_bounds__(BLOCK) k_sssp(PathArgs a) {
   }
 }
 
+// Relax the out-links e0..e1 of v; returns how many frontier bits it turned
+// on.  Zones other than the source are never expanded, so their bits are not
+// set (their labels still drop).
+template <typename T>
+__device__ __forceinline__ int relax_range(int src, int e0, int e1, int first_thru,
+                                           const Edges<T>& ed, typename DT<T>::U* dist,
+                                           unsigned* bm, T du) {
+  using U = typename DT<T>::U;
+  int pushes = 0;
+  for (int b = e0; b < e1; b += kEdgeGroup) {
+    int hh[kEdgeGroup];
+    T ww[kEdgeGroup];
+#pragma unroll
+    for (int j = 0; j < kEdgeGroup; ++j)
+      if (b + j < e1) ed.load(b + j, hh[j], ww[j]);
+#pragma unroll
+    for (int j = 0; j < kEdgeGroup; ++j) {
+      if (b + j >= e1) break;
+      const int h = hh[j];
+      const U nb = DT<T>::bits(DT<T>::add(du, ww[j]));
+      if (nb < vload(dist + h)) {
+        const U old = atomicMin(dist + h, nb);
+        if (nb < old && !(h < first_thru && h != src)) {
+          const unsigned bit = 1u << (h & 31);
+          if (!(vload(bm + (h >> 5)) & bit)) {
+            const unsigned prev = atomicOr(bm + (h >> 5), bit);
+            if (!(prev & bit)) ++pushes;
+          }
+        }
+      }
+    }
+  }
+  return pushes;
+}
+
+__device__ __forceinline__ int warp_sum(int v) {
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
+constexpr long long kMaxIdlePolls = 1ll << 24;  // bound on one warp's idle polling
+constexpr int kMaxRestarts = 64;
+
+// All-origins shortest paths without per-round barriers.  Frontier bitmap
+// word i belongs to warp i mod W; a warp claims its set bits with atomicExch
+// and relaxes those nodes at once, so a label improvement propagates as soon
+// as the owner of the head polls (label correction in the style of the
+// reference's d'Esopo-Pape queue, made parallel).  `pending` counts frontier
+// bits plus claimed-but-unfinished nodes plus reserved pushes: a warp
+// reserves deg(v) before relaxing v's links and releases the unused part
+// after, so the counter never under-counts and a warp may leave once it reads
+// zero.  A final block-wide check that no bit is left makes the result
+// independent of the counter (a premature exit costs a restart only).
+template <typename T, int BLOCK, bool SMEM>
+__global__ void __launch_bounds__(BLOCK) k_sssp_async(PathArgs a) {
+  using U = typename DT<T>::U;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int sh_task;
+  __shared__ int pending;
+  const int n1 = a.g.n1;
+  const int nwords = (n1 + 31) >> 5;
+  unsigned char* base =
+      SMEM ? smem_raw
+           : static_cast<unsigned char*>(a.scratch) + static_cast<size_t>(blockIdx.x) * a.scratch_stride;
+  U* dist = reinterpret_cast<U*>(base);
+  unsigned* bm = reinterpret_cast<unsigned*>(base + align16(sizeof(U) * n1));
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  constexpr int kWarps = BLOCK / 32;
+  const int F = a.g.first_thru;
+  const int my_words = warp < nwords ? (nwords - warp + kWarps - 1) / kWarps : 0;
+
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) sh_task = atomicAdd(a.counter, 1) + a.task_begin;
+    __syncthreads();
+    const int task = sh_task;
+    if (task >= a.task_end) break;
+    const int slot = task / a.num_sources;
+    const int scen = a.scen_list ? a.scen_list[slot] : 0;
+    if (a.state && a.state[scen].done) continue;
+    const int src = a.sources[task - slot * a.num_sources];
+    const Edges<T> ed = edges_of<T>(a, scen);
+    unsigned expanded = 0;
+    int passes = 0;
+
+    for (int v = threadIdx.x; v < n1; v += BLOCK) dist[v] = DT<T>::kInf;
+    for (int i = threadIdx.x; i < nwords; i += BLOCK) bm[i] = 0u;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      dist[src] = DT<T>::bits(T(0));
+      bm[src >> 5] = 1u << (src & 31);
+      pending = 1;
+    }
+    __syncthreads();
+
+    for (int restart = 0;; ++restart) {
+      long long idle = 0;
+      for (;;) {
+        int claimed_any = 0;
+        for (int j0 = 0; j0 < my_words; j0 += 32) {
+          const int j = j0 + lane;
+          const int wi = warp + j * kWarps;
+          unsigned word = 0u;
+          if (j < my_words) {
+            word = vload(bm + wi);
+            if (word) word = atomicExch(bm + wi, 0u);
+          }
+          const int cnt = __popc(word);
+          int incl = cnt;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(kFull, incl, o);
+            if (lane >= o) incl += y;
+          }
+          const int total = __shfl_sync(kFull, incl, 31);
+          if (total == 0) continue;
+          claimed_any = 1;
+          for (int b = 0; b < total; b += 32) {
+            const int jj = b + lane;
+            int owner = 0;
+#pragma unroll
+            for (int step = 16; step >= 1; step >>= 1) {
+              const int probe = __shfl_sync(kFull, incl, owner + step - 1);
+              if (probe <= jj) owner += step;
+            }
+            owner &= 31;
+            const unsigned ow = __shfl_sync(kFull, word, owner);
+            const int oincl = __shfl_sync(kFull, incl, owner);
+            const bool valid = jj < total;
+            int v = 0, e0 = 0, e1 = 0;
+            if (valid) {
+              v = ((warp + (j0 + owner) * kWarps) << 5) + nth_set_bit(ow, jj - (oincl - __popc(ow)));
+              if (!(v < F && v != src)) {
+                e0 = __ldg(a.g.row_ptr + v);
+                e1 = __ldg(a.g.row_ptr + v + 1);
+              }
+            }
+            const int reserve = warp_sum(e1 - e0);
+            const int items = warp_sum(valid ? 1 : 0);
+            if (lane == 0) {
+              atomicAdd(&pending, reserve);
+              __threadfence_block();
+            }
+            __syncwarp();
+            int pushes = 0;
+            if (e1 > e0) pushes = relax_range<T>(src, e0, e1, F, ed, dist, bm, DT<T>::val(vload(dist + v)));
+            expanded += valid ? 1u : 0u;
+            const int used = warp_sum(pushes);
+            __syncwarp();
+            if (lane == 0) {
+              __threadfence_block();
+              atomicAdd(&pending, -(reserve - used + items));
+            }
+          }
+        }
+        if (warp == 0) ++passes;
+        if (!claimed_any) {
+          if (vload(&pending) <= 0) break;
+          if (++idle > kMaxIdlePolls) {
+            if (lane == 0) atomicOr(a.err, kErrRounds);
+            break;
+          }
+          __nanosleep(64);
+        }
+      }
+      __syncthreads();
+      int left = 0;
+      for (int i = threadIdx.x; i < nwords; i += BLOCK) left |= (bm[i] != 0u);
+      if (!__syncthreads_or(left)) break;
+      if (restart >= kMaxRestarts) {
+        if (threadIdx.x == 0) atomicOr(a.err, kErrRounds);
+        break;
+      }
+      // bits remain after every warp left: recount them and resume
+      if (threadIdx.x == 0) pending = 0;
+      __syncthreads();
+      int c = 0;
+      for (int i = threadIdx.x; i < nwords; i += BLOCK) c += __popc(bm[i]);
+      c = warp_sum(c);
+      if (lane == 0) atomicAdd(&pending, c);
+      __syncthreads();
+    }
+    T* out = static_cast<T*>(a.dist) + static_cast<size_t>(task - a.task_begin) * n1;
+    for (int v = threadIdx.x; v < n1; v += BLOCK) out[v] = DT<T>::val(dist[v]);
+    if (a.stats) {
+      for (int o = 16; o >= 1; o >>= 1) expanded += __shfl_down_sync(kFull, expanded, o);
+      if (lane == 0) atomicAdd(a.stats + 2, static_cast<unsigned long long>(expanded));
+      if (threadIdx.x == 0) {
+        atomicAdd(a.stats + 0, static_cast<unsigned long long>(passes));
+        atomicAdd(a.stats + 1, 1ull);
+      }
+    }
+  }
+}
+
 template <typename T, int BLOCK, bool SMEM>
 __global__ void __launch_bounds__(BLOCK) k_aon(PathArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -755,9 +952,16 @@ cudaError_t allow_max_smem(Fn fn) {
   return e;
 }
 
+using PathKernel = void (*)(PathArgs);
+
 template <typename T, int BLOCK, bool SMEM>
-cudaError_t launch_sssp_t(const PathArgs& a, int grid, size_t smem, cudaStream_t s) {
-  auto fn = k_sssp<T, BLOCK, SMEM>;
+PathKernel sssp_kernel(int variant) {
+  return variant == kSsspRounds ? k_sssp<T, BLOCK, SMEM> : k_sssp_async<T, BLOCK, SMEM>;
+}
+
+template <typename T, int BLOCK, bool SMEM>
+cudaError_t launch_sssp_t(const PathArgs& a, int grid, size_t smem, int variant, cudaStream_t s) {
+  PathKernel fn = sssp_kernel<T, BLOCK, SMEM>(variant);
   if (SMEM) {
     cudaError_t e = allow_max_smem(fn);
     if (e != cudaSuccess) return e;
@@ -795,14 +999,14 @@ int max_smem_optin(int device) {
 }
 
 cudaError_t launch_sssp(const PathArgs& a, bool fp64, int grid, int block, bool smem,
-                        cudaStream_t s) {
+                        int variant, cudaStream_t s) {
   const size_t bytes = sssp_smem_bytes(a.g.n1, fp64);
 #define TAPGPU_SSSP_CASE(B)                                                              \
   if (block == B) {                                                                      \
-    if (fp64) return smem ? launch_sssp_t<double, B, true>(a, grid, bytes, s)            \
-                          : launch_sssp_t<double, B, false>(a, grid, bytes, s);          \
-    return smem ? launch_sssp_t<float, B, true>(a, grid, bytes, s)                       \
-                : launch_sssp_t<float, B, false>(a, grid, bytes, s);                     \
+    if (fp64) return smem ? launch_sssp_t<double, B, true>(a, grid, bytes, variant, s)   \
+                          : launch_sssp_t<double, B, false>(a, grid, bytes, variant, s); \
+    return smem ? launch_sssp_t<float, B, true>(a, grid, bytes, variant, s)              \
+                : launch_sssp_t<float, B, false>(a, grid, bytes, variant, s);            \
   }
   TAPGPU_SSSP_CASE(128)
   TAPGPU_SSSP_CASE(256)
@@ -830,8 +1034,8 @@ cudaError_t launch_aon(const PathArgs& a, bool fp64, int grid, int block, bool s
 }
 
 template <typename T, int BLOCK, bool SMEM>
-int occ_sssp_t(size_t smem) {
-  auto fn = k_sssp<T, BLOCK, SMEM>;
+int occ_sssp_t(size_t smem, int variant) {
+  PathKernel fn = sssp_kernel<T, BLOCK, SMEM>(variant);
   if (SMEM && allow_max_smem(fn) != cudaSuccess) return 0;
   int n = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, BLOCK, SMEM ? smem : 0) != cudaSuccess)
@@ -849,12 +1053,14 @@ int occ_aon_t(size_t smem) {
   return n;
 }
 
-int sssp_occupancy(bool fp64, int block, bool smem, int n1) {
+int sssp_occupancy(bool fp64, int block, bool smem, int n1, int variant) {
   const size_t bytes = sssp_smem_bytes(n1, fp64);
 #define TAPGPU_OCC(B)                                                                     \
   if (block == B) {                                                                       \
-    if (fp64) return smem ? occ_sssp_t<double, B, true>(bytes) : occ_sssp_t<double, B, false>(bytes); \
-    return smem ? occ_sssp_t<float, B, true>(bytes) : occ_sssp_t<float, B, false>(bytes);   \
+    if (fp64) return smem ? occ_sssp_t<double, B, true>(bytes, variant)                   \
+                          : occ_sssp_t<double, B, false>(bytes, variant);                 \
+    return smem ? occ_sssp_t<float, B, true>(bytes, variant)                              \
+                : occ_sssp_t<float, B, false>(bytes, variant);                            \
   }
   TAPGPU_OCC(128)
   TAPGPU_OCC(256)

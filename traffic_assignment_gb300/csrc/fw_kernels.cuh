@@ -125,8 +125,13 @@ struct LinkArgs {
 size_t sssp_smem_bytes(int n1, bool fp64);
 size_t aon_smem_bytes(int n1);
 int max_smem_optin(int device);
+// shortest-path kernel variants
+enum : int {
+  kSsspRounds = 1,  // bulk-synchronous label-correction rounds (k_sssp)
+  kSsspAsync = 2,   // warp-owned frontier words, no per-round barrier (k_sssp_async)
+};
 cudaError_t launch_sssp(const PathArgs& a, bool fp64, int grid, int block, bool smem,
-                        cudaStream_t s);
+                        int variant, cudaStream_t s);
 cudaError_t launch_aon(const PathArgs& a, bool fp64, int grid, int block, bool smem,
                        cudaStream_t s);
 // x = loaded volumes (a.pass == 0) or x as given (a.pass == 1); t = BPR(x); weights; state reset
@@ -136,7 +141,7 @@ cudaError_t launch_set_costs(const LinkArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_ls_pass(const LinkArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_ls_fallback(const LinkArgs& a, cudaStream_t s);
 cudaError_t launch_step(const LinkArgs& a, int grid, cudaStream_t s);
-int sssp_occupancy(bool fp64, int block, bool smem, int n1);  // resident CTAs per SM
+int sssp_occupancy(bool fp64, int block, bool smem, int n1, int variant);  // CTAs per SM
 int aon_occupancy(bool fp64, int block, bool smem, int n1);
 
 }  // namespace tapgpu

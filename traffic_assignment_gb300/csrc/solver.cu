@@ -252,13 +252,14 @@ int Ctx::plan_launches() {
   TG_CUDA(cudaGetDeviceProperties(&prop, device));
   num_sms = prop.multiProcessorCount;
   const int optin = max_smem_optin(device);
-  sssp_block = opt.sssp_block > 0 ? opt.sssp_block : 256;
+  sssp_variant = opt.sssp_variant == kSsspRounds ? kSsspRounds : kSsspAsync;
+  sssp_block = opt.sssp_block > 0 ? opt.sssp_block : 512;
   aon_block = opt.aon_block > 0 ? opt.aon_block : 512;
   // leave room for the kernels' static shared memory (a few words)
   const size_t room = optin > 1024 ? static_cast<size_t>(optin - 1024) : 0;
   sssp_smem = sssp_smem_bytes(n1, fp64) <= room && !opt.global_scratch;
   aon_smem = aon_smem_bytes(n1) <= room && !opt.global_scratch;
-  int so = sssp_occupancy(fp64, sssp_block, sssp_smem, n1);
+  int so = sssp_occupancy(fp64, sssp_block, sssp_smem, n1, sssp_variant);
   int ao = aon_occupancy(fp64, aon_block, aon_smem, n1);
   if (so <= 0 || ao <= 0) {
     set_message("no resident CTA fits for the shortest-path kernels");
@@ -298,7 +299,8 @@ int Ctx::enqueue_paths(int nscen, bool load, const uint2* e32p, const double* w6
     TG_CUDA(cudaMemsetAsync(counters, 0, 2 * sizeof(int), stream));
     a.counter = counters;
     if (measuring) TG_TRY(mark(0, true));
-    TG_CUDA(launch_sssp(a, fp64, std::min(sssp_grid, ntask), sssp_block, sssp_smem, stream));
+    TG_CUDA(launch_sssp(a, fp64, std::min(sssp_grid, ntask), sssp_block, sssp_smem, sssp_variant,
+                        stream));
     if (measuring) TG_TRY(mark(0, false));
     a.counter = counters + 1;
     a.scratch_stride = static_cast<long long>(aon_smem_bytes(n1));
@@ -1016,7 +1018,7 @@ int tapgpu_sssp(tapgpu_ctx* ctx, const double* weights, const int64_t* srcs, int
     a.y_fx = c->api_yfx;
     const int optin = tapgpu::max_smem_optin(c->device);
     const bool s_smem = tapgpu::sssp_smem_bytes(n1, true) + 1024 <= static_cast<size_t>(optin);
-    const int occ = tapgpu::sssp_occupancy(true, c->sssp_block, s_smem, n1);
+    const int occ = tapgpu::sssp_occupancy(true, c->sssp_block, s_smem, n1, c->sssp_variant);
     int grid = std::max(1, std::min(occ * c->num_sms, ns));
     if (!s_smem) {
       const size_t need = tapgpu::sssp_smem_bytes(n1, true) * static_cast<size_t>(grid);
@@ -1031,7 +1033,8 @@ int tapgpu_sssp(tapgpu_ctx* ctx, const double* weights, const int64_t* srcs, int
     cudaMemsetAsync(c->counters, 0, 2 * sizeof(int), c->stream);
     a.counter = c->counters;
     a.scratch_stride = static_cast<long long>(tapgpu::sssp_smem_bytes(n1, true));
-    if (tapgpu::launch_sssp(a, true, grid, c->sssp_block, s_smem, c->stream) != cudaSuccess) {
+    if (tapgpu::launch_sssp(a, true, grid, c->sssp_block, s_smem, c->sssp_variant, c->stream) !=
+        cudaSuccess) {
       rc = TAPGPU_ERR_CUDA;
       break;
     }
@@ -1199,7 +1202,7 @@ int tapgpu_profile_iteration(tapgpu_ctx* ctx, int reps, float* ms) {
       break;
     }
     tapgpu::launch_sssp(a, c->fp64, std::min<int64_t>(c->sssp_grid, tasks), c->sssp_block,
-                        c->sssp_smem, c->stream);
+                        c->sssp_smem, c->sssp_variant, c->stream);
     cudaEventRecord(ev[1], c->stream);
     a.counter = c->counters + 1;
     a.scratch_stride = static_cast<long long>(tapgpu::aon_smem_bytes(c->n1));

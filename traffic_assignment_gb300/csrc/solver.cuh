@@ -101,6 +101,7 @@ struct Ctx {
 
   // launch shapes
   int sssp_block = 256, aon_block = 512, link_grid = 0;
+  int sssp_variant = kSsspAsync;
   bool sssp_smem = true, aon_smem = true;
   int sssp_grid = 0, aon_grid = 0;
 
