@@ -41,7 +41,7 @@ def test_aon_matches_oracle(built_lib, grid416):
             assert _rel(y, ref) < 1e-12
 
 
-VARIANTS = ["rounds", "async"]
+VARIANTS = ["rounds", "async", "nearfar"]
 
 
 @pytest.mark.parametrize("variant", VARIANTS)

@@ -46,7 +46,7 @@ class Options(C.Structure):
                 ("aon_block", C.c_int), ("iters_per_launch", C.c_int), ("use_graphs", C.c_int),
                 ("chunk_tasks", C.c_int64), ("record_tape", C.c_int),
                 ("tape_capacity", C.c_int), ("global_scratch", C.c_int),
-                ("sssp_variant", C.c_int)]
+                ("sssp_variant", C.c_int), ("nf_delta", C.c_double)]
 
 
 class Result(C.Structure):

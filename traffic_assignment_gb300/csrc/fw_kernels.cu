@@ -116,6 +116,46 @@ __device__ __forceinline__ Edges<double> edges_of<double>(const PathArgs& a, int
   return Edges<double>{a.g.head, a.w64 + static_cast<size_t>(scen) * a.g.m};
 }
 
+// In-links of a node in reverse-star order (link id ascending).  FP32 paths
+// read one packed {tail, weight bits} record per in-link; the link id is
+// fetched only for the chosen predecessor.
+template <typename T>
+struct RevEdges;
+template <>
+struct RevEdges<float> {
+  const uint2* r;
+  const int* in_link;
+  __device__ __forceinline__ void load(int i, int& u, float& w) const {
+    const uint2 x = __ldg(r + i);
+    u = static_cast<int>(x.x);
+    w = __uint_as_float(x.y);
+  }
+  __device__ __forceinline__ int link(int i) const { return __ldg(in_link + i); }
+};
+template <>
+struct RevEdges<double> {
+  const int* in_link;
+  const int* tail;
+  const double* w;
+  __device__ __forceinline__ void load(int i, int& u, double& x) const {
+    const int k = __ldg(in_link + i);
+    u = __ldg(tail + k);
+    x = __ldg(w + k);
+  }
+  __device__ __forceinline__ int link(int i) const { return __ldg(in_link + i); }
+};
+
+template <typename T>
+__device__ __forceinline__ RevEdges<T> rev_edges_of(const PathArgs& a, int scen);
+template <>
+__device__ __forceinline__ RevEdges<float> rev_edges_of<float>(const PathArgs& a, int scen) {
+  return RevEdges<float>{a.r32 + static_cast<size_t>(scen) * a.g.m, a.g.in_link};
+}
+template <>
+__device__ __forceinline__ RevEdges<double> rev_edges_of<double>(const PathArgs& a, int scen) {
+  return RevEdges<double>{a.g.in_link, a.g.tail, a.w64 + static_cast<size_t>(scen) * a.g.m};
+}
+
 constexpr int kEdgeGroup = 4;  // edge records fetched together before relaxing
 
 // Relax the out-links of v; returns 1 if any head label dropped.  The edge
@@ -453,6 +493,260 @@ __global__ void __launch_bounds__(BLOCK) k_sssp_async(PathArgs a) {
   }
 }
 
+// Relax the out-links e0..e1 of v for the near-far variant: a head whose new
+// label is below the phase threshold goes to the near bitmap (counted in
+// the returned pushes), any other head to the far bitmap.
+template <typename T>
+__device__ __forceinline__ int relax_range_nf(int src, int e0, int e1, int first_thru,
+                                              const Edges<T>& ed, typename DT<T>::U* dist,
+                                              unsigned* near, unsigned* far, T du,
+                                              typename DT<T>::U thr_bits) {
+  using U = typename DT<T>::U;
+  int pushes = 0;
+  for (int b = e0; b < e1; b += kEdgeGroup) {
+    int hh[kEdgeGroup];
+    T ww[kEdgeGroup];
+#pragma unroll
+    for (int j = 0; j < kEdgeGroup; ++j)
+      if (b + j < e1) ed.load(b + j, hh[j], ww[j]);
+#pragma unroll
+    for (int j = 0; j < kEdgeGroup; ++j) {
+      if (b + j >= e1) break;
+      const int h = hh[j];
+      const U nb = DT<T>::bits(DT<T>::add(du, ww[j]));
+      if (nb < vload(dist + h)) {
+        const U old = atomicMin(dist + h, nb);
+        if (nb < old && !(h < first_thru && h != src)) {
+          const unsigned bit = 1u << (h & 31);
+          if (nb < thr_bits) {
+            if (!(vload(near + (h >> 5)) & bit)) {
+              const unsigned prev = atomicOr(near + (h >> 5), bit);
+              if (!(prev & bit)) ++pushes;
+            }
+          } else if (!(vload(far + (h >> 5)) & bit)) {
+            atomicOr(far + (h >> 5), bit);
+          }
+        }
+      }
+    }
+  }
+  return pushes;
+}
+
+// All-origins shortest paths, near-far ordering: labels below a threshold T
+// are corrected asynchronously (warp-owned near-bitmap words, as in
+// k_sssp_async); heads at or above T wait in a far bitmap.  When no near work
+// is left, one block-wide step raises T to (smallest far label + delta) and
+// promotes the far nodes below it.  Nodes are then expanded close to once
+// (the ordering of delta-stepping) instead of once per improvement.  A far
+// node may also sit in the near set; expanding it twice is harmless.  The
+// result is the same least fixed point as every other variant.
+template <typename T, int BLOCK, bool SMEM>
+__global__ void __launch_bounds__(BLOCK) k_sssp_nf(PathArgs a) {
+  using U = typename DT<T>::U;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int sh_task;
+  __shared__ int pending;
+  __shared__ U sh_min;
+  const int n1 = a.g.n1;
+  const int nwords = (n1 + 31) >> 5;
+  unsigned char* base =
+      SMEM ? smem_raw
+           : static_cast<unsigned char*>(a.scratch) + static_cast<size_t>(blockIdx.x) * a.scratch_stride;
+  U* dist = reinterpret_cast<U*>(base);
+  unsigned* near = reinterpret_cast<unsigned*>(base + align16(sizeof(U) * n1));
+  unsigned* far = near + nwords;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  constexpr int kWarps = BLOCK / 32;
+  const int F = a.g.first_thru;
+  const int my_words = warp < nwords ? (nwords - warp + kWarps - 1) / kWarps : 0;
+  const T delta = static_cast<T>(a.nf_delta);
+
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) sh_task = atomicAdd(a.counter, 1) + a.task_begin;
+    __syncthreads();
+    const int task = sh_task;
+    if (task >= a.task_end) break;
+    const int slot = task / a.num_sources;
+    const int scen = a.scen_list ? a.scen_list[slot] : 0;
+    if (a.state && a.state[scen].done) continue;
+    const int src = a.sources[task - slot * a.num_sources];
+    const Edges<T> ed = edges_of<T>(a, scen);
+    unsigned expanded = 0;
+    int phases = 0;
+
+    for (int v = threadIdx.x; v < n1; v += BLOCK) dist[v] = DT<T>::kInf;
+    for (int i = threadIdx.x; i < 2 * nwords; i += BLOCK) near[i] = 0u;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      dist[src] = DT<T>::bits(T(0));
+      near[src >> 5] = 1u << (src & 31);
+      pending = 1;
+    }
+    __syncthreads();
+    U thr = DT<T>::bits(delta);
+
+    for (;;) {  // phases
+      // -- asynchronous correction of the near set ---------------------------
+      long long idle = 0;
+      for (;;) {
+        int claimed_any = 0;
+        for (int j0 = 0; j0 < my_words; j0 += 32) {
+          const int j = j0 + lane;
+          const int wi = warp + j * kWarps;
+          unsigned word = 0u;
+          if (j < my_words) {
+            word = vload(near + wi);
+            if (word) word = atomicExch(near + wi, 0u);
+          }
+          const int cnt = __popc(word);
+          int incl = cnt;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(kFull, incl, o);
+            if (lane >= o) incl += y;
+          }
+          const int total = __shfl_sync(kFull, incl, 31);
+          if (total == 0) continue;
+          claimed_any = 1;
+          for (int b = 0; b < total; b += 32) {
+            const int jj = b + lane;
+            int owner = 0;
+#pragma unroll
+            for (int step = 16; step >= 1; step >>= 1) {
+              const int probe = __shfl_sync(kFull, incl, owner + step - 1);
+              if (probe <= jj) owner += step;
+            }
+            owner &= 31;
+            const unsigned ow = __shfl_sync(kFull, word, owner);
+            const int oincl = __shfl_sync(kFull, incl, owner);
+            const bool valid = jj < total;
+            int v = 0, e0 = 0, e1 = 0;
+            if (valid) {
+              v = ((warp + (j0 + owner) * kWarps) << 5) + nth_set_bit(ow, jj - (oincl - __popc(ow)));
+              if (!(v < F && v != src)) {
+                e0 = __ldg(a.g.row_ptr + v);
+                e1 = __ldg(a.g.row_ptr + v + 1);
+              }
+            }
+            const int reserve = warp_sum(e1 - e0);
+            const int items = warp_sum(valid ? 1 : 0);
+            if (lane == 0) {
+              atomicAdd(&pending, reserve);
+              __threadfence_block();
+            }
+            __syncwarp();
+            int pushes = 0;
+            if (e1 > e0)
+              pushes = relax_range_nf<T>(src, e0, e1, F, ed, dist, near, far,
+                                         DT<T>::val(vload(dist + v)), thr);
+            expanded += valid ? 1u : 0u;
+            const int used = warp_sum(pushes);
+            __syncwarp();
+            if (lane == 0) {
+              __threadfence_block();
+              atomicAdd(&pending, -(reserve - used + items));
+            }
+          }
+        }
+        if (!claimed_any) {
+          if (vload(&pending) <= 0) break;
+          if (++idle > kMaxIdlePolls) {
+            if (lane == 0) atomicOr(a.err, kErrRounds);
+            break;
+          }
+          __nanosleep(32);
+        }
+      }
+      __syncthreads();
+      // -- phase step: near set empty?  then raise the threshold --------------
+      int left = 0;
+      for (int i = threadIdx.x; i < nwords; i += BLOCK) left |= (near[i] != 0u);
+      if (__syncthreads_or(left)) {  // a warp left early: recount and resume
+        if (threadIdx.x == 0) pending = 0;
+        __syncthreads();
+        int c = 0;
+        for (int i = threadIdx.x; i < nwords; i += BLOCK) c += __popc(near[i]);
+        c = warp_sum(c);
+        if (lane == 0) atomicAdd(&pending, c);
+        __syncthreads();
+        if (++phases > a.max_rounds) {
+          if (threadIdx.x == 0) atomicOr(a.err, kErrRounds);
+          break;
+        }
+        continue;
+      }
+      // smallest far label (far bits of nodes already settled below it are dropped)
+      if (threadIdx.x == 0) sh_min = DT<T>::kInf;
+      __syncthreads();
+      // A far node whose label is now below the old threshold got that label
+      // by a relaxation that also queued it in the near set, so it has been
+      // expanded with it: its far bit is stale.
+      U mn = DT<T>::kInf;
+      for (int i = threadIdx.x; i < nwords; i += BLOCK) {
+        const unsigned w = far[i];
+        if (!w) continue;
+        unsigned keep = 0u, ww = w;
+        while (ww) {
+          const int bpos = __ffs(ww) - 1;
+          ww &= ww - 1;
+          const U dv = dist[(i << 5) + bpos];
+          if (dv >= thr) {
+            keep |= 1u << bpos;
+            if (dv < mn) mn = dv;
+          }
+        }
+        if (keep != w) far[i] = keep;
+      }
+      if (mn != DT<T>::kInf) atomicMin(&sh_min, mn);
+      __syncthreads();
+      const U fmin = sh_min;
+      if (fmin == DT<T>::kInf) break;  // nothing left: labels are final
+      thr = DT<T>::bits(DT<T>::add(DT<T>::val(fmin), delta));
+      if (thr <= fmin) thr = fmin + 1;  // delta absorbed: still make progress
+      // promote far nodes below the new threshold
+      int moved = 0;
+      for (int i = threadIdx.x; i < nwords; i += BLOCK) {
+        const unsigned w = far[i];
+        if (!w) continue;
+        unsigned take = 0u;
+        unsigned ww = w;
+        while (ww) {
+          const int bpos = __ffs(ww) - 1;
+          ww &= ww - 1;
+          if (dist[(i << 5) + bpos] < thr) take |= 1u << bpos;
+        }
+        if (take) {
+          far[i] = w & ~take;
+          near[i] = take;
+          moved += __popc(take);
+        }
+      }
+      if (threadIdx.x == 0) pending = 0;
+      __syncthreads();
+      moved = warp_sum(moved);
+      if (lane == 0 && moved) atomicAdd(&pending, moved);
+      __syncthreads();
+      if (++phases > a.max_rounds) {
+        if (threadIdx.x == 0) atomicOr(a.err, kErrRounds);
+        break;
+      }
+    }
+    T* out = static_cast<T*>(a.dist) + static_cast<size_t>(task - a.task_begin) * n1;
+    for (int v = threadIdx.x; v < n1; v += BLOCK) out[v] = DT<T>::val(dist[v]);
+    if (a.stats) {
+      for (int o = 16; o >= 1; o >>= 1) expanded += __shfl_down_sync(kFull, expanded, o);
+      if (lane == 0) atomicAdd(a.stats + 2, static_cast<unsigned long long>(expanded));
+      if (threadIdx.x == 0) {
+        atomicAdd(a.stats + 0, static_cast<unsigned long long>(phases));
+        atomicAdd(a.stats + 1, 1ull);
+      }
+    }
+  }
+}
+
 template <typename T, int BLOCK, bool SMEM>
 __global__ void __launch_bounds__(BLOCK) k_aon(PathArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -479,6 +773,7 @@ __global__ void __launch_bounds__(BLOCK) k_aon(PathArgs a) {
     const int sidx = task - slot * a.num_sources;
     const int src = a.sources[sidx];
     const Edges<T> ed = edges_of<T>(a, scen);
+    const RevEdges<T> rv = rev_edges_of<T>(a, scen);
     const T* din = static_cast<const T*>(a.dist) + static_cast<size_t>(task - a.task_begin) * n1;
 
     for (int v = threadIdx.x; v < n1; v += BLOCK) dS[v] = din[v];
@@ -491,15 +786,24 @@ __global__ void __launch_bounds__(BLOCK) k_aon(PathArgs a) {
       const T dv = dS[v];
       if (v != src && DT<T>::bits(dv) != DT<T>::kInf) {
         p = -2;
+        const int i0 = __ldg(a.g.in_ptr + v);
         const int i1 = __ldg(a.g.in_ptr + v + 1);
-        for (int i = __ldg(a.g.in_ptr + v); i < i1; ++i) {
-          const int k = __ldg(a.g.in_link + i);
-          const int u = __ldg(a.g.tail + k);
-          if (u < F && u != src) continue;
-          const T du = dS[u];
-          if (du < dv && DT<T>::add(du, ed.weight(k)) == dv) {
-            p = k;
-            break;
+        for (int b = i0; b < i1 && p == -2; b += kEdgeGroup) {
+          int uu[kEdgeGroup];
+          T ww[kEdgeGroup];
+#pragma unroll
+          for (int j = 0; j < kEdgeGroup; ++j)
+            if (b + j < i1) rv.load(b + j, uu[j], ww[j]);
+#pragma unroll
+          for (int j = 0; j < kEdgeGroup; ++j) {
+            if (b + j >= i1) break;
+            const int u = uu[j];
+            if (u < F && u != src) continue;
+            const T du = dS[u];
+            if (du < dv && DT<T>::add(du, ww[j]) == dv) {
+              p = rv.link(b + j);
+              break;
+            }
           }
         }
         if (p == -2) pend = 1;
@@ -679,9 +983,11 @@ __device__ __forceinline__ bool last_block(unsigned* arrive) {
 
 // shortest-path weight of link k of the scenario at offset i - k
 __device__ __forceinline__ void write_weights(const LinkArgs& a, size_t i, int k, double t) {
-  if (a.e32)
-    a.e32[i] = make_uint2(static_cast<unsigned>(__ldg(a.head + k)),
-                          __float_as_uint(__double2float_rn(t)));
+  if (a.e32) {
+    const unsigned bits = __float_as_uint(__double2float_rn(t));
+    a.e32[i] = make_uint2(static_cast<unsigned>(__ldg(a.head + k)), bits);
+    a.r32[i - k + __ldg(a.rpos + k)] = make_uint2(static_cast<unsigned>(__ldg(a.tail + k)), bits);
+  }
   if (a.w64) a.w64[i] = t;
 }
 
@@ -956,7 +1262,9 @@ using PathKernel = void (*)(PathArgs);
 
 template <typename T, int BLOCK, bool SMEM>
 PathKernel sssp_kernel(int variant) {
-  return variant == kSsspRounds ? k_sssp<T, BLOCK, SMEM> : k_sssp_async<T, BLOCK, SMEM>;
+  if (variant == kSsspRounds) return k_sssp<T, BLOCK, SMEM>;
+  if (variant == kSsspAsync) return k_sssp_async<T, BLOCK, SMEM>;
+  return k_sssp_nf<T, BLOCK, SMEM>;
 }
 
 template <typename T, int BLOCK, bool SMEM>

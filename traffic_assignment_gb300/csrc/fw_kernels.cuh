@@ -70,6 +70,7 @@ struct Demand {
 struct PathArgs {
   Graph g;
   const uint2* e32;             // [S][m] {head, f32 weight bits} when fp32 paths
+  const uint2* r32;             // [S][m] {tail, f32 weight bits} in reverse-star order
   const double* w64;            // [S][m] when fp64 paths
   const int* sources;           // source nodes
   int num_sources;
@@ -90,6 +91,7 @@ struct PathArgs {
   void* scratch;                // per-CTA global scratch when the smem variant does not fit
   long long scratch_stride;     // bytes per CTA
   unsigned long long* stats;    // optional [4]: rounds, tasks, node expansions, -
+  double nf_delta;              // near-far threshold step (label units)
 };
 
 struct LinkArgs {
@@ -103,7 +105,10 @@ struct LinkArgs {
   double* d;                    // [S][m]
   unsigned long long* y_fx;     // [S][m]
   uint2* e32;                   // [S][m] packed fp32 edge records, or nullptr
+  uint2* r32;                   // [S][m] packed fp32 reverse records (with e32)
   const int* head;              // [m] head node of each link (for e32)
+  const int* tail;              // [m] tail node of each link (for r32)
+  const int* rpos;              // [m] reverse-star slot of each link (for r32)
   double* w64;                  // [S][m] or nullptr
   double* dtdx;                 // [S][m] or nullptr (derivative of the BPR cost)
   double* partials;             // [S][gridDim.x][kNumSums]
@@ -129,6 +134,7 @@ int max_smem_optin(int device);
 enum : int {
   kSsspRounds = 1,  // bulk-synchronous label-correction rounds (k_sssp)
   kSsspAsync = 2,   // warp-owned frontier words, no per-round barrier (k_sssp_async)
+  kSsspNearFar = 3, // asynchronous near set below a rising threshold (k_sssp_nf)
 };
 cudaError_t launch_sssp(const PathArgs& a, bool fp64, int grid, int block, bool smem,
                         int variant, cudaStream_t s);

@@ -164,6 +164,7 @@ PathArgs Ctx::path_args(int nscen_slots) const {
   a.scratch = path_scratch;
   a.scratch_stride = 0;
   a.stats = timing ? path_stats : nullptr;
+  a.nf_delta = nf_delta;
   return a;
 }
 
@@ -180,7 +181,10 @@ LinkArgs Ctx::link_args(int nscen) const {
   a.d = d;
   a.y_fx = yfx;
   a.e32 = fp64 ? nullptr : e32;
+  a.r32 = fp64 ? nullptr : r32;
   a.head = head;
+  a.tail = tail;
+  a.rpos = rpos;
   a.w64 = fp64 ? w64 : nullptr;
   a.dtdx = dtdx;
   a.partials = partials;
@@ -201,12 +205,13 @@ LinkArgs Ctx::link_args(int nscen) const {
 int Ctx::ensure_scenarios(int S) {
   if (S <= S_cap) return TAPGPU_OK;
   // release the old per-scenario arrays
-  void* olds[] = {cap, x, t, d, dtdx, yfx, e32, w64, state, partials, arrive, trace, scen_list,
+  void* olds[] = {cap, x, t, d, dtdx, yfx, e32, r32, w64, state, partials, arrive, trace, scen_list,
                   x_hist, d_hist, lam_hist};
   for (void* p : olds) free_owned(this, p);
   cap = x = t = d = dtdx = nullptr;
   yfx = nullptr;
   e32 = nullptr;
+  r32 = nullptr;
   w64 = nullptr;
   state = nullptr;
   partials = nullptr;
@@ -223,7 +228,10 @@ int Ctx::ensure_scenarios(int S) {
   if (fp64)
     TG_TRY(alloc_n(&w64, sm));
   else
+  {
     TG_TRY(alloc_n(&e32, sm));
+    TG_TRY(alloc_n(&r32, sm));
+  }
   if (opt.record_tape) TG_TRY(alloc_n(&dtdx, sm));
   TG_TRY(alloc_n(&state, static_cast<size_t>(S)));
   TG_TRY(alloc_n(&partials, static_cast<size_t>(S) * link_grid * kNumSums));
@@ -252,7 +260,9 @@ int Ctx::plan_launches() {
   TG_CUDA(cudaGetDeviceProperties(&prop, device));
   num_sms = prop.multiProcessorCount;
   const int optin = max_smem_optin(device);
-  sssp_variant = opt.sssp_variant == kSsspRounds ? kSsspRounds : kSsspAsync;
+  sssp_variant = (opt.sssp_variant >= kSsspRounds && opt.sssp_variant <= kSsspNearFar)
+                     ? opt.sssp_variant
+                     : kSsspNearFar;
   sssp_block = opt.sssp_block > 0 ? opt.sssp_block : 512;
   aon_block = opt.aon_block > 0 ? opt.aon_block : 512;
   // leave room for the kernels' static shared memory (a few words)
@@ -278,13 +288,14 @@ int Ctx::plan_launches() {
   return TAPGPU_OK;
 }
 
-int Ctx::enqueue_paths(int nscen, bool load, const uint2* e32p, const double* w64p,
+int Ctx::enqueue_paths(int nscen, bool load, const uint2* e32p, const uint2* r32p, const double* w64p,
                        unsigned long long* ydst, bool use_state) {
   const int64_t tasks = static_cast<int64_t>(nscen) * Z;
   for (int64_t t0 = 0; t0 < tasks; t0 += dist_tasks) {
     const int64_t t1 = std::min(tasks, t0 + dist_tasks);
     PathArgs a = path_args(nscen);
     a.e32 = e32p;
+    a.r32 = r32p;
     a.w64 = w64p;
     a.y_fx = ydst;
     a.do_load = load ? 1 : 0;
@@ -323,7 +334,7 @@ void Ctx::count_launches(long long n) {
 
 int Ctx::enqueue_iteration(int nscen) {
   measuring = true;
-  int rc = enqueue_paths(nscen, true, e32, w64, yfx, true);
+  int rc = enqueue_paths(nscen, true, e32, r32, w64, yfx, true);
   measuring = false;
   TG_TRY(rc);
   LinkArgs la = link_args(nscen);
@@ -347,7 +358,7 @@ int Ctx::enqueue_initial(int nscen, bool warm) {
   if (!warm) {
     TG_CUDA(launch_set_costs(la, link_grid, stream));
     count_launches(1);
-    TG_TRY(enqueue_paths(nscen, true, e32, w64, yfx, true));
+    TG_TRY(enqueue_paths(nscen, true, e32, r32, w64, yfx, true));
     la.pass = 0;
   } else {
     la.pass = 1;
@@ -550,6 +561,12 @@ static int create_impl(const tapgpu_network* net, const tapgpu_demand* dem,
   // tap/tap_frankwolfe_pthread.c:654-669 zero capacity -> smallest nonzero capacity
   for (int k = 0; k < M; ++k)
     if (!(c->h_cap[k] > 0.0)) c->h_cap[k] = min_cap;
+  {
+    double s = 0.0;
+    for (int k = 0; k < M; ++k) s += c->h_fft[k];
+    const double mean = s / M;
+    c->nf_delta = opt.nf_delta > 0 ? opt.nf_delta : (mean > 0 ? 8.0 * mean : 1.0);
+  }
 
   std::vector<int> rp(n1 + 1, 0), ip_in(n1 + 1, 0), inl(M);
   for (int k = 0; k < M; ++k) {
@@ -560,9 +577,13 @@ static int create_impl(const tapgpu_network* net, const tapgpu_demand* dem,
     rp[v + 1] += rp[v];
     ip_in[v + 1] += ip_in[v];
   }
+  c->h_rpos.resize(M);
   {
     std::vector<int> fill(ip_in.begin(), ip_in.end() - 1);
-    for (int k = 0; k < M; ++k) inl[fill[c->h_head[k]]++] = k;
+    for (int k = 0; k < M; ++k) {
+      c->h_rpos[k] = fill[c->h_head[k]];
+      inl[fill[c->h_head[k]]++] = k;
+    }
   }
 
   TG_TRY(c->alloc_n(&c->row_ptr, n1 + 1));
@@ -570,6 +591,7 @@ static int create_impl(const tapgpu_network* net, const tapgpu_demand* dem,
   TG_TRY(c->alloc_n(&c->tail, M));
   TG_TRY(c->alloc_n(&c->in_ptr, n1 + 1));
   TG_TRY(c->alloc_n(&c->in_link, M));
+  TG_TRY(c->alloc_n(&c->rpos, M));
   TG_TRY(c->alloc_n(&c->fft, M));
   TG_TRY(c->alloc_n(&c->alpha, M));
   TG_TRY(c->alloc_n(&c->beta, M));
@@ -579,6 +601,7 @@ static int create_impl(const tapgpu_network* net, const tapgpu_demand* dem,
   TG_CUDA(cudaMemcpy(c->tail, c->h_tail.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
   TG_CUDA(cudaMemcpy(c->in_ptr, ip_in.data(), sizeof(int) * (n1 + 1), cudaMemcpyHostToDevice));
   TG_CUDA(cudaMemcpy(c->in_link, inl.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
+  TG_CUDA(cudaMemcpy(c->rpos, c->h_rpos.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
   TG_CUDA(cudaMemcpy(c->fft, c->h_fft.data(), sizeof(double) * M, cudaMemcpyHostToDevice));
   TG_CUDA(cudaMemcpy(c->alpha, c->h_alpha.data(), sizeof(double) * M, cudaMemcpyHostToDevice));
   TG_CUDA(cudaMemcpy(c->beta, c->h_beta.data(), sizeof(double) * M, cudaMemcpyHostToDevice));
@@ -647,6 +670,7 @@ static int create_impl(const tapgpu_network* net, const tapgpu_demand* dem,
   c->dist_tasks = std::min<int64_t>(chunk, std::max<int64_t>(Z, 1) * 4096);
   TG_TRY(c->alloc(&c->dist, tb * c->dist_tasks));
   TG_TRY(c->alloc_n(&c->api_e32, M));
+  TG_TRY(c->alloc_n(&c->api_r32, M));
   TG_TRY(c->alloc_n(&c->api_w64, M));
   TG_TRY(c->alloc_n(&c->api_yfx, M));
   TG_TRY(c->ensure_scenarios(1));
@@ -930,7 +954,7 @@ int tapgpu_solve_scenarios(tapgpu_ctx* ctx, int num_scen, const int64_t* scen_pt
     // once and start every scenario from it
     tapgpu::LinkArgs la = c->link_args(1);
     TG_CUDA(tapgpu::launch_set_costs(la, c->link_grid, c->stream));
-    TG_TRY(c->enqueue_paths(1, true, c->e32, c->w64, c->yfx, true));
+    TG_TRY(c->enqueue_paths(1, true, c->e32, c->r32, c->w64, c->yfx, true));
     for (int s = 1; s < num_scen; ++s)
       TG_CUDA(cudaMemcpyAsync(c->yfx + static_cast<size_t>(s) * M, c->yfx,
                               sizeof(unsigned long long) * M, cudaMemcpyDeviceToDevice,
@@ -951,7 +975,7 @@ int tapgpu_solve_scenarios(tapgpu_ctx* ctx, int num_scen, const int64_t* scen_pt
 
 static int to_device_weights(Ctx* c, const double* weights) {
   std::vector<double> w(c->M);
-  std::vector<uint2> wf(c->M);
+  std::vector<uint2> wf(c->M), wr(c->M);
   for (int k = 0; k < c->M; ++k) {
     const double v = weights[c->perm[k]];
     if (!(v >= 0) || std::isinf(v)) {
@@ -963,7 +987,16 @@ static int to_device_weights(Ctx* c, const double* weights) {
     unsigned bits;
     std::memcpy(&bits, &f, sizeof bits);
     wf[k] = make_uint2(static_cast<unsigned>(c->h_head[k]), bits);
+    wr[c->h_rpos[k]] = make_uint2(static_cast<unsigned>(c->h_tail[k]), bits);
   }
+  {
+    double s = 0.0;
+    for (int k = 0; k < c->M; ++k) s += w[k];
+    const double mean = s / c->M;
+    c->api_nf_delta = c->opt.nf_delta > 0 ? c->opt.nf_delta : (mean > 0 ? 8.0 * mean : 1.0);
+  }
+  TG_CUDA(cudaMemcpyAsync(c->api_r32, wr.data(), sizeof(uint2) * c->M, cudaMemcpyHostToDevice,
+                          c->stream));
   TG_CUDA(cudaMemcpyAsync(c->api_w64, w.data(), sizeof(double) * c->M, cudaMemcpyHostToDevice,
                           c->stream));
   TG_CUDA(cudaMemcpyAsync(c->api_e32, wf.data(), sizeof(uint2) * c->M, cudaMemcpyHostToDevice,
@@ -1016,6 +1049,7 @@ int tapgpu_sssp(tapgpu_ctx* ctx, const double* weights, const int64_t* srcs, int
     a.do_load = 0;
     a.pred_out = c->pred_buf;
     a.y_fx = c->api_yfx;
+    a.nf_delta = c->api_nf_delta;
     const int optin = tapgpu::max_smem_optin(c->device);
     const bool s_smem = tapgpu::sssp_smem_bytes(n1, true) + 1024 <= static_cast<size_t>(optin);
     const int occ = tapgpu::sssp_occupancy(true, c->sssp_block, s_smem, n1, c->sssp_variant);
@@ -1081,8 +1115,13 @@ int tapgpu_aon(tapgpu_ctx* ctx, const double* weights, double* volume) {
   TG_TRY(to_device_weights(c, weights));
   TG_CUDA(cudaMemsetAsync(c->api_yfx, 0, sizeof(unsigned long long) * c->M, c->stream));
   TG_CUDA(cudaMemsetAsync(c->err, 0, sizeof(int), c->stream));
-  TG_TRY(c->enqueue_paths(1, true, c->fp64 ? nullptr : c->api_e32, c->fp64 ? c->api_w64 : nullptr,
-                          c->api_yfx, false));
+  const double solver_delta = c->nf_delta;
+  c->nf_delta = c->api_nf_delta;
+  const int rc = c->enqueue_paths(1, true, c->fp64 ? nullptr : c->api_e32,
+                                  c->fp64 ? nullptr : c->api_r32, c->fp64 ? c->api_w64 : nullptr,
+                                  c->api_yfx, false);
+  c->nf_delta = solver_delta;
+  TG_TRY(rc);
   TG_TRY(c->sync_check());
   std::vector<unsigned long long> y(c->M);
   TG_CUDA(cudaMemcpy(y.data(), c->api_yfx, sizeof(unsigned long long) * c->M,
@@ -1196,6 +1235,7 @@ int tapgpu_profile_iteration(tapgpu_ctx* ctx, int reps, float* ms) {
     a.counter = c->counters;
     a.scratch_stride = static_cast<long long>(tapgpu::sssp_smem_bytes(c->n1, c->fp64));
     a.e32 = c->fp64 ? nullptr : c->e32;
+    a.r32 = c->fp64 ? nullptr : c->r32;
     a.w64 = c->fp64 ? c->w64 : nullptr;
     if (tasks > c->dist_tasks) {
       rc = TAPGPU_ERR_UNSUPPORTED;

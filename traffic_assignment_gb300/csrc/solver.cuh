@@ -47,6 +47,9 @@ struct Ctx {
   double *cap = nullptr, *x = nullptr, *t = nullptr, *d = nullptr, *dtdx = nullptr;
   unsigned long long* yfx = nullptr;
   uint2* e32 = nullptr;  // packed {head, f32 weight} per scenario and link
+  uint2* r32 = nullptr;  // packed {tail, f32 weight} per scenario, reverse-star order
+  int* rpos = nullptr;   // reverse-star slot of each link
+  std::vector<int> h_rpos;
   double* w64 = nullptr;
   ScenState* state = nullptr;
   double* partials = nullptr;
@@ -70,6 +73,7 @@ struct Ctx {
   unsigned long long* path_stats = nullptr;  // [4] rounds, tasks, expansions (timing on)
   // buffers of the one-shot API (weights in both precisions, loaded volumes)
   uint2* api_e32 = nullptr;
+  uint2* api_r32 = nullptr;
   double* api_w64 = nullptr;
   unsigned long long* api_yfx = nullptr;
 
@@ -102,6 +106,8 @@ struct Ctx {
   // launch shapes
   int sssp_block = 256, aon_block = 512, link_grid = 0;
   int sssp_variant = kSsspAsync;
+  double nf_delta = 1.0;      // near-far threshold step for the solver's costs
+  double api_nf_delta = 1.0;  // the same for the weights of the one-shot API
   bool sssp_smem = true, aon_smem = true;
   int sssp_grid = 0, aon_grid = 0;
 
@@ -123,7 +129,7 @@ struct Ctx {
   LinkArgs link_args(int nscen) const;
 
   // enqueue helpers (stream ordered, capturable)
-  int enqueue_paths(int nscen, bool load, const uint2* e32p, const double* w64p,
+  int enqueue_paths(int nscen, bool load, const uint2* e32p, const uint2* r32p, const double* w64p,
                     unsigned long long* ydst, bool use_state);
   int enqueue_iteration(int nscen);
   int enqueue_initial(int nscen, bool warm);

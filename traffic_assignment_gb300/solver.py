@@ -57,7 +57,8 @@ class Solver:
                  device: int = 0, sssp_block: int = 0, aon_block: int = 0,
                  iters_per_launch: int = 0, use_graphs: bool = True, chunk_tasks: int = 0,
                  record_tape: bool = False, tape_capacity: int = 0,
-                 global_scratch: bool = False, sssp_variant: str = "default"):
+                 global_scratch: bool = False, sssp_variant: str = "default",
+                 nf_delta: float = 0.0):
         self.L = K.load()
         self.net = net
         self.dem = dem
@@ -73,7 +74,8 @@ class Solver:
         opt.record_tape = 1 if record_tape else 0
         opt.tape_capacity = tape_capacity
         opt.global_scratch = 1 if global_scratch else 0
-        opt.sssp_variant = {"default": 0, "rounds": 1, "async": 2}[sssp_variant]
+        opt.sssp_variant = {"default": 0, "rounds": 1, "async": 2, "nearfar": 3}[sssp_variant]
+        opt.nf_delta = float(nf_delta)
         self.precision = "fp32" if opt.precision == K.TAPGPU_FP32_PATHS else "fp64"
         keep: list = []
         ns = _net_struct(net, keep)
