@@ -238,7 +238,7 @@ typedef struct tapgpu_options_s {
   int global_scratch;    /* 1: per-CTA labels in global memory even when shared memory fits */
   int sssp_variant;      /* 0 default; 1 bulk-synchronous rounds; 2 asynchronous warp-owned
                             frontier; 3 asynchronous near set below a rising threshold */
-  double nf_delta;       /* threshold step of variant 3 in cost units; 0 = 8 x mean link cost */
+  double nf_delta;       /* threshold step of variant 3 in cost units; 0 = 16 x mean link cost */
 } tapgpu_options;
 
 typedef struct tapgpu_result_s {

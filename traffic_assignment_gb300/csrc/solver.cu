@@ -263,7 +263,7 @@ int Ctx::plan_launches() {
   sssp_variant = (opt.sssp_variant >= kSsspRounds && opt.sssp_variant <= kSsspNearFar)
                      ? opt.sssp_variant
                      : kSsspNearFar;
-  sssp_block = opt.sssp_block > 0 ? opt.sssp_block : 512;
+  sssp_block = opt.sssp_block > 0 ? opt.sssp_block : (sssp_variant == kSsspNearFar ? 256 : 512);
   aon_block = opt.aon_block > 0 ? opt.aon_block : 512;
   // leave room for the kernels' static shared memory (a few words)
   const size_t room = optin > 1024 ? static_cast<size_t>(optin - 1024) : 0;
@@ -565,7 +565,7 @@ static int create_impl(const tapgpu_network* net, const tapgpu_demand* dem,
     double s = 0.0;
     for (int k = 0; k < M; ++k) s += c->h_fft[k];
     const double mean = s / M;
-    c->nf_delta = opt.nf_delta > 0 ? opt.nf_delta : (mean > 0 ? 8.0 * mean : 1.0);
+    c->nf_delta = opt.nf_delta > 0 ? opt.nf_delta : (mean > 0 ? 16.0 * mean : 1.0);
   }
 
   std::vector<int> rp(n1 + 1, 0), ip_in(n1 + 1, 0), inl(M);
@@ -993,7 +993,7 @@ static int to_device_weights(Ctx* c, const double* weights) {
     double s = 0.0;
     for (int k = 0; k < c->M; ++k) s += w[k];
     const double mean = s / c->M;
-    c->api_nf_delta = c->opt.nf_delta > 0 ? c->opt.nf_delta : (mean > 0 ? 8.0 * mean : 1.0);
+    c->api_nf_delta = c->opt.nf_delta > 0 ? c->opt.nf_delta : (mean > 0 ? 16.0 * mean : 1.0);
   }
   TG_CUDA(cudaMemcpyAsync(c->api_r32, wr.data(), sizeof(uint2) * c->M, cudaMemcpyHostToDevice,
                           c->stream));
