@@ -79,7 +79,7 @@ EXPORTED = [
     "tapgpu_get_link_flows", "tapgpu_get_trace", "tapgpu_set_capacity",
     "tapgpu_solve_scenarios", "tapgpu_sssp", "tapgpu_aon", "tapgpu_stream",
     "tapgpu_profile_iteration", "tapgpu_run_iterations", "tapgpu_set_timing",
-    "tapgpu_get_timing", "tapgpu_get_path_stats",
+    "tapgpu_get_timing", "tapgpu_get_path_stats", "tapgpu_sssp_labels_noalloc",
 ]
 EXPORTED_DATA = ["num_cores", "num_threads", "using_fermi_architecture"]
 
@@ -128,6 +128,9 @@ def load(path: str | None = None):
     L.tapgpu_get_timing.argtypes = [vp, F64P, I64P, I64P]
     L.tapgpu_get_path_stats.argtypes = [vp, I64P]
     L.tapgpu_get_path_stats.restype = C.c_int
+    L.tapgpu_sssp_labels_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_int32, vp, vp, vp, vp,
+                                             C.c_int32, vp, vp]
+    L.tapgpu_sssp_labels_noalloc.restype = C.c_int
     for fn in ("tapgpu_create", "tapgpu_solve", "tapgpu_solve_begin", "tapgpu_solve_advance",
                "tapgpu_get_link_flows", "tapgpu_get_trace", "tapgpu_set_capacity",
                "tapgpu_solve_scenarios", "tapgpu_sssp", "tapgpu_aon",

@@ -25,7 +25,7 @@ OBJ = os.path.join(OUT, "obj")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INC, "-I", CSRC,
               "--expt-relaxed-constexpr"]
-CU_SOURCES = ["fw_kernels.cu", "solver.cu", "linkops.cu", "adjoint.cu"]
+CU_SOURCES = ["fw_kernels.cu", "solver.cu", "linkops.cu", "adjoint.cu", "noalloc.cu"]
 CXX_SOURCES = ["capi.cpp"]
 C_SOURCES = ["tntp_io.c"]
 
