@@ -239,6 +239,10 @@ typedef struct tapgpu_options_s {
   int sssp_variant;      /* 0 default; 1 bulk-synchronous rounds; 2 asynchronous warp-owned
                             frontier; 3 asynchronous near set below a rising threshold */
   double nf_delta;       /* threshold step of variant 3 in cost units; 0 = 16 x mean link cost */
+  int line_search;       /* 0: the reference's 2^-k rule; 1: exact root of the directional
+                            derivative (differentiable step sizes, for the adjoint) */
+  int tape_checkpoint;   /* with record_tape: flows kept every this many iterations and
+                            recomputed in between by the adjoint (0 = sqrt(tape_capacity)) */
 } tapgpu_options;
 
 typedef struct tapgpu_result_s {
@@ -319,6 +323,20 @@ int tapgpu_run_iterations(tapgpu_ctx *ctx, int iters);
  * the solver launched since the reset. */
 int tapgpu_set_timing(tapgpu_ctx *ctx, int on);
 int tapgpu_get_timing(tapgpu_ctx *ctx, double *ms, int64_t *counts, int64_t *kernel_launches);
+/* Reverse-mode derivative of the final VHT of scenario s with respect to the
+ * link capacities, through every iteration of its last solve (no counterpart
+ * in the reference).  Needs a context created with record_tape and
+ * tape_capacity >= the iterations run.  The all-or-nothing loads are held
+ * fixed (they are piecewise constant in the capacities); with
+ * line_search = 1 the step sizes are differentiated by the implicit-function
+ * rule, with the reference's 2^-k rule they are held fixed.  grad: [M] in the
+ * caller's link order; vht (optional): the VHT the gradient belongs to. */
+int tapgpu_adjoint_vht(tapgpu_ctx *ctx, int scenario, double *grad, double *vht);
+/* One iteration of the recorded tape: direction d_k [M], step lambda_k, and
+ * the flows x_k [M] when k is a checkpoint (k % tape_checkpoint == 0). */
+int tapgpu_get_tape(tapgpu_ctx *ctx, int scenario, int iteration, double *x_checkpoint,
+                    double *direction, double *lambda);
+
 /* Shortest-path work counters gathered while timing is on: out[0] label
  * correction rounds, out[1] (scenario, origin) tasks, out[2] node expansions. */
 int tapgpu_get_path_stats(tapgpu_ctx *ctx, int64_t *out);

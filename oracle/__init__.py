@@ -77,6 +77,11 @@ def lib():
         L.orc_objective.argtypes = [C.POINTER(Problem), F64P, F64P]
         L.orc_bpr.restype = C.c_double
         L.orc_bpr.argtypes = [C.c_double] * 5
+        L.orc_replay_vht.restype = C.c_double
+        L.orc_replay_vht.argtypes = [C.POINTER(Problem), F64P, C.c_int, F64P, F64P, F64P]
+        L.orc_adjoint_vht.restype = C.c_int
+        L.orc_adjoint_vht.argtypes = [C.POINTER(Problem), F64P, C.c_int, F64P, F64P, F64P,
+                                      F64P]
         _LIB = L
     return _LIB
 
@@ -166,6 +171,32 @@ def objective(net, x, capacity=None):
     b = _Bound(net, _empty_demand(net), capacity)
     xa = np.ascontiguousarray(x, np.float64)
     return lib().orc_objective(C.byref(b.prob), _p(b.keep["cap"], F64P), _p(xa, F64P))
+
+
+def replay_vht(net, capacity, x0, loads):
+    """VHT after the frozen-load FW map (loads [K][M], exact steps); also the steps."""
+    b = _Bound(net, _empty_demand(net), capacity)
+    Y = np.ascontiguousarray(loads, np.float64)
+    k = Y.shape[0]
+    xa = np.ascontiguousarray(x0, np.float64)
+    lam = np.zeros(max(k, 1))
+    v = lib().orc_replay_vht(C.byref(b.prob), _p(b.keep["cap"], F64P), k, _p(xa, F64P),
+                             _p(Y, F64P), _p(lam, F64P))
+    return v, lam[:k]
+
+
+def adjoint_vht(net, capacity, x0, directions, lambdas):
+    """FP64 reverse sweep of the frozen-load FW map on a tape -> dVHT/dcapacity."""
+    b = _Bound(net, _empty_demand(net), capacity)
+    D = np.ascontiguousarray(directions, np.float64)
+    lam = np.ascontiguousarray(lambdas, np.float64)
+    xa = np.ascontiguousarray(x0, np.float64)
+    g = np.zeros(net.num_links)
+    rc = lib().orc_adjoint_vht(C.byref(b.prob), _p(b.keep["cap"], F64P), D.shape[0],
+                               _p(xa, F64P), _p(D, F64P), _p(lam, F64P), _p(g, F64P))
+    if rc != 0:
+        raise RuntimeError(f"oracle adjoint failed rc={rc}")
+    return g
 
 
 def _empty_demand(net):

@@ -46,12 +46,13 @@ def _stale(out, srcs):
 def build_oracle(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     out = os.path.join(BUILD, "liboracle_tap.so")
-    srcs = [os.path.join(HERE, "oracle_tap.c"), os.path.join(HERE, "oracle_tap.h")]
+    srcs = [os.path.join(HERE, "oracle_tap.c"), os.path.join(HERE, "oracle_adjoint.c"),
+            os.path.join(HERE, "oracle_tap.h")]
     if force or _stale(out, srcs):
         tmp = out + ".tmp"
         # no fused multiply-add: the Arm host would otherwise round differently
         _run(["gcc", *CFLAGS, "-ffp-contract=off", "-std=c11", "-fPIC", "-shared", "-o", tmp,
-              srcs[0], "-lm"])
+              srcs[0], srcs[1], "-lm"])
         os.replace(tmp, out)
     return out
 

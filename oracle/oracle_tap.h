@@ -98,6 +98,13 @@ int orc_frankwolfe(const orc_problem_t *p, int num_threads, const double *x0,
                    int max_iters, double target_relgap, double *x_out, double *t_out,
                    orc_iter_t *trace, int trace_cap, double *summary);
 
+/* oracle_adjoint.c: FP64 CPU reference of the VHT adjoint (frozen loads Y [K][M],
+ * exact steps): the replay for finite differences and the reverse sweep on a tape */
+double orc_replay_vht(const orc_problem_t *p, const double *cap, int K, const double *x0,
+                      const double *Y, double *lam_out);
+int orc_adjoint_vht(const orc_problem_t *p, const double *cap, int K, const double *x0,
+                    const double *D, const double *lam, double *grad);
+
 #ifdef __cplusplus
 }
 #endif

@@ -46,7 +46,8 @@ class Options(C.Structure):
                 ("aon_block", C.c_int), ("iters_per_launch", C.c_int), ("use_graphs", C.c_int),
                 ("chunk_tasks", C.c_int64), ("record_tape", C.c_int),
                 ("tape_capacity", C.c_int), ("global_scratch", C.c_int),
-                ("sssp_variant", C.c_int), ("nf_delta", C.c_double)]
+                ("sssp_variant", C.c_int), ("nf_delta", C.c_double),
+                ("line_search", C.c_int), ("tape_checkpoint", C.c_int)]
 
 
 class Result(C.Structure):
@@ -80,6 +81,7 @@ EXPORTED = [
     "tapgpu_solve_scenarios", "tapgpu_sssp", "tapgpu_aon", "tapgpu_stream",
     "tapgpu_profile_iteration", "tapgpu_run_iterations", "tapgpu_set_timing",
     "tapgpu_get_timing", "tapgpu_get_path_stats", "tapgpu_sssp_labels_noalloc",
+    "tapgpu_adjoint_vht", "tapgpu_get_tape",
 ]
 EXPORTED_DATA = ["num_cores", "num_threads", "using_fermi_architecture"]
 
@@ -131,6 +133,10 @@ def load(path: str | None = None):
     L.tapgpu_sssp_labels_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_int32, vp, vp, vp, vp,
                                              C.c_int32, vp, vp]
     L.tapgpu_sssp_labels_noalloc.restype = C.c_int
+    L.tapgpu_adjoint_vht.argtypes = [vp, C.c_int, F64P, F64P]
+    L.tapgpu_adjoint_vht.restype = C.c_int
+    L.tapgpu_get_tape.argtypes = [vp, C.c_int, C.c_int, F64P, F64P, F64P]
+    L.tapgpu_get_tape.restype = C.c_int
     for fn in ("tapgpu_create", "tapgpu_solve", "tapgpu_solve_begin", "tapgpu_solve_advance",
                "tapgpu_get_link_flows", "tapgpu_get_trace", "tapgpu_set_capacity",
                "tapgpu_solve_scenarios", "tapgpu_sssp", "tapgpu_aon",

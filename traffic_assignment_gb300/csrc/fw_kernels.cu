@@ -22,6 +22,8 @@
 //              (tap/tap_frankwolfe_pthread.c:737-739, tap/tap_functions.c:55-65).
 #include "fw_kernels.cuh"
 
+#include "bpr.cuh"
+
 #include <cfloat>
 #include <cstdio>
 #include <mutex>
@@ -905,42 +907,18 @@ __device__ __forceinline__ double pow2neg(int e) {
   return __longlong_as_double(static_cast<long long>(1023 - e) << 52);
 }
 
-__device__ __forceinline__ double int_pow(double r, int n) {
-  double acc = 1.0, b = r;
-  while (n) {
-    if (n & 1) acc = __dmul_rn(acc, b);
-    n >>= 1;
-    if (n) b = __dmul_rn(b, b);
-  }
-  return acc;
-}
-
-__device__ __forceinline__ double pow_p(double r, double beta, unsigned char ip) {
-  return ip != 255 ? int_pow(r, ip) : pow(r, beta);
-}
-
-// tap/tap_functions.c:55-65
+// tap/tap_functions.c:55-65, 112-126 (see bpr.cuh)
 __device__ __forceinline__ double bpr(double fft, double alpha, double beta, unsigned char ip,
                                       double cap, double q) {
-  const double p = pow_p(__ddiv_rn(q, cap), beta, ip);
-  return __dmul_rn(fft, __dadd_rn(1.0, __dmul_rn(alpha, p)));
+  return bprf::cost(fft, alpha, beta, ip, cap, q);
 }
-
-// d t / d q of the BPR cost
 __device__ __forceinline__ double bpr_dq(double fft, double alpha, double beta, unsigned char ip,
                                          double cap, double q) {
-  if (beta == 0.0) return 0.0;
-  const double r = q / cap;
-  const double p1 = ip != 255 ? (ip >= 1 ? int_pow(r, ip - 1) : 0.0) : pow(r, beta - 1.0);
-  return fft * alpha * beta * p1 / cap;
+  return bprf::dcost_dq(fft, alpha, beta, ip, cap, q);
 }
-
-// tap/tap_functions.c:112-126
 __device__ __forceinline__ double integral(double fft, double alpha, double beta, unsigned char ip,
                                            double cap, double q) {
-  if (!(beta >= 0)) return 0.0;
-  const double a = __ddiv_rn(__ddiv_rn(alpha, pow_p(cap, beta, ip)), __dadd_rn(beta, 1.0));
-  return __dmul_rn(__dmul_rn(q, fft), __dadd_rn(1.0, __dmul_rn(a, pow_p(q, beta, ip))));
+  return bprf::integral(fft, alpha, beta, ip, cap, q);
 }
 
 template <int N, int BLOCK>
@@ -1042,7 +1020,15 @@ __global__ void __launch_bounds__(kLinkBlock) k_set_free_flow(LinkArgs a) {
   }
 }
 
-__device__ void ls_decide(ScenState& st, const double* tot, int first_e, int pass, double total_demand) {
+// candidate step j of a pass: 2^-(e0+j) (reference rule) or the j-th of 12
+// interior points of the current bracket (exact root)
+__device__ __forceinline__ double ls_candidate(int mode, int e0, double lo, double hi, int j) {
+  if (mode == kLsExact) return lo + (hi - lo) * static_cast<double>(j + 1) / (kLsPerPass + 1);
+  return pow2neg(e0 + j);
+}
+
+__device__ void ls_decide(ScenState& st, const double* tot, int first_e, int pass, double total_demand,
+                          int mode) {
   if (pass == 0) {
     const double g0 = tot[0];
     st.g0 = g0;
@@ -1064,6 +1050,30 @@ __device__ void ls_decide(ScenState& st, const double* tot, int first_e, int pas
       st.ls_pending = 0;
       return;
     }
+    st.ls_lo = 0.0;
+    st.ls_glo = g0;
+    st.ls_hi = 1.0;
+    st.ls_ghi = tot[3];
+  }
+  if (mode == kLsExact) {
+    // g rises with lambda (convex objective): keep the sign change bracketed
+    const double lo = st.ls_lo, hi = st.ls_hi;
+    for (int j = 0; j < kLsPerPass; ++j) {
+      const double lam = ls_candidate(mode, 0, lo, hi, j);
+      if (tot[4 + j] > 0) {
+        st.ls_hi = lam;
+        st.ls_ghi = tot[4 + j];
+        break;
+      }
+      st.ls_lo = lam;
+      st.ls_glo = tot[4 + j];
+    }
+    if (pass + 1 >= kLsExactPasses || st.ls_hi - st.ls_lo <= 1e-15 * st.ls_hi) {
+      const double den = st.ls_glo - st.ls_ghi;
+      st.lambda = den < 0 ? st.ls_lo + (st.ls_hi - st.ls_lo) * (st.ls_glo / den) : st.ls_lo;
+      st.ls_pending = 0;
+    }
+    return;
   }
   for (int j = 0; j < kLsPerPass; ++j) {
     if (tot[4 + j] <= 0) {
@@ -1085,6 +1095,8 @@ __global__ void __launch_bounds__(kLinkBlock) k_ls_pass(LinkArgs a) {
   if (a.pass > 0 && !st.ls_pending) return;
   const size_t off = static_cast<size_t>(scen) * a.m;
   const int e0 = a.pass == 0 ? 1 : st.ls_next;
+  const double blo = a.pass == 0 ? 0.0 : st.ls_lo;
+  const double bhi = a.pass == 0 ? 1.0 : st.ls_hi;
   double acc[kNumSums];
 #pragma unroll
   for (int i = 0; i < kNumSums; ++i) acc[i] = 0.0;
@@ -1109,7 +1121,7 @@ __global__ void __launch_bounds__(kLinkBlock) k_ls_pass(LinkArgs a) {
     }
 #pragma unroll
     for (int j = 0; j < kLsPerPass; ++j) {
-      const double lam = pow2neg(e0 + j);
+      const double lam = ls_candidate(a.ls_mode, e0, blo, bhi, j);
       const double q = __dadd_rn(x, __dmul_rn(lam, d));
       acc[4 + j] = __dadd_rn(acc[4 + j], __dmul_rn(bpr(fft, al, be, ip, c, q), d));
     }
@@ -1128,7 +1140,7 @@ __global__ void __launch_bounds__(kLinkBlock) k_ls_pass(LinkArgs a) {
     for (unsigned b = 0; b < gridDim.x; ++b)
       for (int i = 0; i < kNumSums; ++i)
         tot[i] = __dadd_rn(tot[i], vload(p0 + b * kNumSums + i));
-    ls_decide(st, tot, e0, a.pass, a.total_demand);
+    ls_decide(st, tot, e0, a.pass, a.total_demand, a.ls_mode);
     a.arrive[scen] = 0u;
   }
 }
@@ -1141,6 +1153,14 @@ __global__ void __launch_bounds__(1024) k_ls_fallback(LinkArgs a) {
   const int scen = scen_of(a);
   ScenState& st = a.state[scen];
   if (st.done || !st.ls_pending) return;
+  if (a.ls_mode == kLsExact) {  // bracket already tight: interpolate
+    if (threadIdx.x == 0) {
+      const double den = st.ls_glo - st.ls_ghi;
+      st.lambda = den < 0 ? st.ls_lo + (st.ls_hi - st.ls_lo) * (st.ls_glo / den) : st.ls_lo;
+      st.ls_pending = 0;
+    }
+    return;
+  }
   const size_t off = static_cast<size_t>(scen) * a.m;
   const double* cap = a.cap + off;
   for (int e = st.ls_next; e <= kLsMaxHalvings; ++e) {
@@ -1183,17 +1203,19 @@ __global__ void __launch_bounds__(kLinkBlock) k_step(LinkArgs a) {
   const size_t off = static_cast<size_t>(scen) * a.m;
   const double lam = st.lambda;
   const int it = st.iter;
-  const bool tape = a.x_hist && it < a.hist_cap;
+  // adjoint tape: every direction, the flows only every ckpt_every iterations
+  const bool tape = a.d_hist && it < a.hist_cap;
+  const bool ckpt = tape && (it % a.ckpt_every == 0);
   const size_t hoff = tape ? (static_cast<size_t>(scen) * a.hist_cap + it) * a.m : 0;
+  const size_t nck = static_cast<size_t>(a.hist_cap / a.ckpt_every + 1);
+  const size_t xoff = ckpt ? (static_cast<size_t>(scen) * nck + it / a.ckpt_every) * a.m : 0;
   const double* cap = a.cap + off;
   double acc[1] = {0.0};
   for (int k = blockIdx.x * kLinkBlock + threadIdx.x; k < a.m; k += gridDim.x * kLinkBlock) {
     const double x0 = a.x[off + k];
     const double d = a.d[off + k];
-    if (tape) {
-      a.x_hist[hoff + k] = x0;
-      a.d_hist[hoff + k] = d;
-    }
+    if (tape) a.d_hist[hoff + k] = d;
+    if (ckpt) a.x_hist[xoff + k] = x0;
     const double x = __dadd_rn(x0, __dmul_rn(lam, d));
     a.x[off + k] = x;
     const double fft = a.lp.fft[k], al = a.lp.alpha[k], be = a.lp.beta[k], c = cap[k];

@@ -56,7 +56,15 @@ struct ScenState {
   double target_relgap;
   double relgap, best_lb, obj, gap, lambda, vht, avg_excess, g0;
   double vht_end;  // VHT at the current x with the current costs
+  double ls_lo, ls_hi, ls_glo, ls_ghi;  // exact line search: bracket of the root of g
 };
+
+// line-search modes
+enum : int {
+  kLsReference = 0,  // largest 2^-k with g(2^-k) <= 0 (tap/tap_functions.c:469-507)
+  kLsExact = 1,      // root of g on [0, 1] (differentiable: used by the adjoint)
+};
+constexpr int kLsExactPasses = 14;  // bracket shrinks 13x per pass
 
 struct Demand {
   const int* od_ptr;            // [num_sources+1]
@@ -120,10 +128,12 @@ struct LinkArgs {
   double total_demand;
   int pass;                     // line-search pass index
   int* err;
-  double* x_hist;               // [S][hist_cap][m] flows before each step (adjoint tape)
-  double* d_hist;               // [S][hist_cap][m] directions
+  double* x_hist;               // [S][hist_cap / ckpt_every + 1][m] flows at checkpoints
+  double* d_hist;               // [S][hist_cap][m] directions (adjoint tape)
   double* lam_hist;             // [S][hist_cap]
   int hist_cap;
+  int ckpt_every;               // flows kept every ckpt_every iterations
+  int ls_mode;                  // kLsReference or kLsExact
 };
 
 // launch helpers (implemented in fw_kernels.cu)

@@ -5,6 +5,8 @@
 // assignment, a fixed tree per block and a fixed-order final pass.
 #include "linkops.cuh"
 
+#include "bpr.cuh"
+
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -17,31 +19,12 @@ constexpr int kBlock = 256;
 constexpr int kMaxLambdas = 32;
 constexpr unsigned kFull = 0xffffffffu;
 
-__device__ __forceinline__ double int_pow(double r, int n) {
-  double acc = 1.0, b = r;
-  while (n) {
-    if (n & 1) acc = __dmul_rn(acc, b);
-    n >>= 1;
-    if (n) b = __dmul_rn(b, b);
-  }
-  return acc;
-}
-
-__device__ __forceinline__ double pow_p(double r, double beta, unsigned char ip) {
-  return ip != 255 ? int_pow(r, ip) : pow(r, beta);
-}
-
 __device__ __forceinline__ double bpr(const LinkArrays& l, int k, double q) {
-  const double p = pow_p(__ddiv_rn(q, l.cap[k]), l.beta[k], l.ipow[k]);
-  return __dmul_rn(l.fft[k], __dadd_rn(1.0, __dmul_rn(l.alpha[k], p)));
+  return bprf::cost(l.fft[k], l.alpha[k], l.beta[k], l.ipow[k], l.cap[k], q);
 }
 
 __device__ __forceinline__ double integral(const LinkArrays& l, int k, double q) {
-  const double beta = l.beta[k];
-  if (!(beta >= 0)) return 0.0;
-  const double a = __ddiv_rn(__ddiv_rn(l.alpha[k], pow_p(l.cap[k], beta, l.ipow[k])),
-                             __dadd_rn(beta, 1.0));
-  return __dmul_rn(__dmul_rn(q, l.fft[k]), __dadd_rn(1.0, __dmul_rn(a, pow_p(q, beta, l.ipow[k]))));
+  return bprf::integral(l.fft[k], l.alpha[k], l.beta[k], l.ipow[k], l.cap[k], q);
 }
 
 __global__ void __launch_bounds__(kBlock) k_costs(LinkArrays l, const double* x, double* t, int m) {

@@ -199,6 +199,8 @@ LinkArgs Ctx::link_args(int nscen) const {
   a.d_hist = d_hist;
   a.lam_hist = lam_hist;
   a.hist_cap = hist_cap;
+  a.ckpt_every = ckpt_every;
+  a.ls_mode = ls_mode;
   return a;
 }
 
@@ -242,7 +244,10 @@ int Ctx::ensure_scenarios(int S) {
   TG_TRY(alloc_n(&scen_list, static_cast<size_t>(S)));
   if (opt.record_tape && opt.tape_capacity > 0) {
     hist_cap = opt.tape_capacity;
-    TG_TRY(alloc_n(&x_hist, sm * hist_cap));
+    ckpt_every = opt.tape_checkpoint > 0
+                     ? opt.tape_checkpoint
+                     : std::max(1, static_cast<int>(std::ceil(std::sqrt(double(hist_cap)))));
+    TG_TRY(alloc_n(&x_hist, sm * (hist_cap / ckpt_every + 1)));
     TG_TRY(alloc_n(&d_hist, sm * hist_cap));
     TG_TRY(alloc_n(&lam_hist, static_cast<size_t>(S) * hist_cap));
   }
@@ -260,6 +265,7 @@ int Ctx::plan_launches() {
   TG_CUDA(cudaGetDeviceProperties(&prop, device));
   num_sms = prop.multiProcessorCount;
   const int optin = max_smem_optin(device);
+  ls_mode = opt.line_search == kLsExact ? kLsExact : kLsReference;
   sssp_variant = (opt.sssp_variant >= kSsspRounds && opt.sssp_variant <= kSsspNearFar)
                      ? opt.sssp_variant
                      : kSsspNearFar;
@@ -339,7 +345,8 @@ int Ctx::enqueue_iteration(int nscen) {
   TG_TRY(rc);
   LinkArgs la = link_args(nscen);
   TG_TRY(mark(2, true));
-  for (int p = 0; p < kLsPasses; ++p) {
+  const int passes = ls_mode == kLsExact ? kLsExactPasses : kLsPasses;
+  for (int p = 0; p < passes; ++p) {
     la.pass = p;
     TG_CUDA(launch_ls_pass(la, link_grid, stream));
   }
@@ -348,7 +355,7 @@ int Ctx::enqueue_iteration(int nscen) {
   TG_TRY(mark(3, true));
   TG_CUDA(launch_step(la, link_grid, stream));
   TG_TRY(mark(3, false));
-  count_launches(kLsPasses + 2);
+  count_launches(passes + 2);
   return TAPGPU_OK;
 }
 
@@ -736,10 +743,6 @@ static void fill_result(const ScenState& s, int err_bits, tapgpu_result* r) {
 }  // namespace tapgpu
 
 using tapgpu::Ctx;
-
-struct tapgpu_ctx {
-  Ctx* c;
-};
 
 extern "C" {
 

@@ -60,6 +60,12 @@ struct Ctx {
   std::vector<int> h_scen_list;
   double *x_hist = nullptr, *d_hist = nullptr, *lam_hist = nullptr;
   int hist_cap = 0;
+  int ckpt_every = 1;
+  int ls_mode = kLsReference;
+  // adjoint work buffers (allocated on first use)
+  double *adj_xbar = nullptr, *adj_cbar = nullptr, *adj_seg = nullptr, *adj_part = nullptr;
+  double* adj_scal = nullptr;
+  unsigned* adj_arrive = nullptr;
 
   // scratch
   void* dist = nullptr;
@@ -139,3 +145,8 @@ struct Ctx {
 };
 
 }  // namespace tapgpu
+
+// the opaque handle of the C ABI
+struct tapgpu_ctx {
+  tapgpu::Ctx* c;
+};

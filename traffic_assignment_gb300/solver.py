@@ -58,7 +58,8 @@ class Solver:
                  iters_per_launch: int = 0, use_graphs: bool = True, chunk_tasks: int = 0,
                  record_tape: bool = False, tape_capacity: int = 0,
                  global_scratch: bool = False, sssp_variant: str = "default",
-                 nf_delta: float = 0.0):
+                 nf_delta: float = 0.0, line_search: str = "reference",
+                 tape_checkpoint: int = 0):
         self.L = K.load()
         self.net = net
         self.dem = dem
@@ -76,6 +77,8 @@ class Solver:
         opt.global_scratch = 1 if global_scratch else 0
         opt.sssp_variant = {"default": 0, "rounds": 1, "async": 2, "nearfar": 3}[sssp_variant]
         opt.nf_delta = float(nf_delta)
+        opt.line_search = {"reference": 0, "exact": 1}[line_search]
+        opt.tape_checkpoint = int(tape_checkpoint)
         self.precision = "fp32" if opt.precision == K.TAPGPU_FP32_PATHS else "fp64"
         keep: list = []
         ns = _net_struct(net, keep)
@@ -177,6 +180,23 @@ class Solver:
                                               int(max_iters), float(target_relgap),
                                               None if xa is None else K.ptr(xa, K.F64P), res))
         return [SolveResult(r.as_dict()) for r in res]
+
+    def adjoint_vht(self, scenario: int = 0):
+        """(VHT, dVHT/dcapacity [M]) of the last solve (needs record_tape)."""
+        g = np.zeros(self.m)
+        v = np.zeros(1)
+        K.check(self.L.tapgpu_adjoint_vht(self.h, scenario, K.ptr(g, K.F64P), K.ptr(v, K.F64P)))
+        return float(v[0]), g
+
+    def tape(self, iteration: int, scenario: int = 0, with_flows: bool = False):
+        """(x_k or None, d_k, lambda_k) of the recorded solve."""
+        d = np.zeros(self.m)
+        lam = np.zeros(1)
+        x = np.zeros(self.m) if with_flows else None
+        K.check(self.L.tapgpu_get_tape(self.h, scenario, iteration,
+                                       None if x is None else K.ptr(x, K.F64P),
+                                       K.ptr(d, K.F64P), K.ptr(lam, K.F64P)))
+        return x, d, float(lam[0])
 
     def stream_ptr(self) -> int:
         return int(self.L.tapgpu_stream(self.h) or 0)
