@@ -143,12 +143,13 @@ def measured_peaks():
 
 
 def profile_traffic():
-    """DRAM bytes per full shortest-path launch, from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "k_sssp_grid10k.md")
+    """DRAM bytes per shortest-path task (label write-out dominates), from the
+    committed ncu summary of the near-far kernel on the batched 10k-node case."""
+    p = os.path.join(ROOT, "profiles", "k_sssp_nf_grid10k_batched.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
-        if line.startswith("traffic_bytes_per_full_launch:"):
+        if line.startswith("traffic_bytes_per_task:"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
@@ -292,15 +293,19 @@ def run_ours(args, rank, world, local_rank):
     d2h = S * m * 16 + S * 96
     assert len(outs) == S and all(q["error_bits"] == 0 for q in res2)
 
-    # roofline of the shortest-path kernel: Z (12 M + 8 N) bytes per scenario-iteration
+    # roofline of the shortest-path kernel: 12 M + 8 N bytes per (scenario, origin)
+    # task, averaged over the launches of the timed steps (the last label chunk
+    # of a step is a partial one)
     Z, N, M = net.num_zones, net.num_nodes, m
-    tasks_per_launch = min(S * Z, solver_chunk_tasks(solver, S * Z))
-    bytes_per_launch = (tasks_per_launch / Z) * Z * (12 * M + 8 * N)
-    sssp_avg_ms = tm["sssp_ms"] / max(1, tm["sssp_launches"])
+    launches = max(1, tm["sssp_launches"])
+    tasks_per_launch = S * Z * args.steps / launches
+    bytes_per_launch = tasks_per_launch * (12 * M + 8 * N)
+    sssp_avg_ms = tm["sssp_ms"] / launches
     achieved = bytes_per_launch / (sssp_avg_ms / 1e3) / 1e9
     peaks, peak_kind = measured_peaks()
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    traffic = profile_traffic()
+    per_task = profile_traffic()
+    traffic = None if per_task is None else per_task * tasks_per_launch
 
     line = None
     if rank == 0:
@@ -329,9 +334,14 @@ def run_ours(args, rank, world, local_rank):
                                     for k in ("sssp", "aon", "line_search", "step")},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "k_sssp", "peak_kind": f"{peak_kind} hbm_gbs",
+                         "kernel": "k_sssp_nf", "peak_kind": f"{peak_kind} hbm_gbs",
                          "algorithmic_bytes_per_launch": bytes_per_launch,
-                         "avg_launch_ms": sssp_avg_ms},
+                         "tasks_per_launch": tasks_per_launch,
+                         "avg_launch_ms": sssp_avg_ms,
+                         "traffic_source": "ncu dram__bytes_read+write per task of a "
+                                           "16,000-task launch x tasks_per_launch",
+                         "note": "the algorithmic bytes are edge records and labels served "
+                                 "from L1/L2; the kernel is instruction-issue bound"},
             "cpu_baseline": cpu,
             "clocks": clocks,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d / e2e_iters,
@@ -362,12 +372,6 @@ def profile_case(kind):
         tm = s.timing()
     print(json.dumps({"profile_case": kind, "iterations": r["iterations"], **tm}))
     return 0
-
-
-def solver_chunk_tasks(solver, tasks):
-    """Tasks per shortest-path launch (the label buffer holds 2 GiB by default)."""
-    per_task = (solver.n1) * (4 if solver.precision == "fp32" else 8)
-    return max(1, (2 << 30) // per_task)
 
 
 def main():

@@ -337,8 +337,11 @@ int tapgpu_adjoint_vht(tapgpu_ctx *ctx, int scenario, double *grad, double *vht)
 int tapgpu_get_tape(tapgpu_ctx *ctx, int scenario, int iteration, double *x_checkpoint,
                     double *direction, double *lambda);
 
-/* Shortest-path work counters gathered while timing is on: out[0] label
- * correction rounds, out[1] (scenario, origin) tasks, out[2] node expansions. */
+/* Shortest-path work counters gathered while timing is on (out has 5
+ * entries): out[0] label correction rounds or near-far phases, out[1]
+ * (scenario, origin) tasks, out[2] node expansions, and for the near-far
+ * kernel out[3] idle polls of warps that found no near work and out[4]
+ * warp batches of up to 32 expansions. */
 int tapgpu_get_path_stats(tapgpu_ctx *ctx, int64_t *out);
 
 /* No counterpart in the reference.  All-origins FP64 shortest-path labels for

@@ -577,6 +577,7 @@ __global__ void __launch_bounds__(BLOCK) k_sssp_nf(PathArgs a) {
     const int src = a.sources[task - slot * a.num_sources];
     const Edges<T> ed = edges_of<T>(a, scen);
     unsigned expanded = 0;
+    unsigned long long polls = 0, batches = 0;
     int phases = 0;
 
     for (int v = threadIdx.x; v < n1; v += BLOCK) dist[v] = DT<T>::kInf;
@@ -639,6 +640,7 @@ __global__ void __launch_bounds__(BLOCK) k_sssp_nf(PathArgs a) {
               atomicAdd(&pending, reserve);
               __threadfence_block();
             }
+            ++batches;
             __syncwarp();
             int pushes = 0;
             if (e1 > e0)
@@ -655,6 +657,7 @@ __global__ void __launch_bounds__(BLOCK) k_sssp_nf(PathArgs a) {
         }
         if (!claimed_any) {
           if (vload(&pending) <= 0) break;
+          ++polls;
           if (++idle > kMaxIdlePolls) {
             if (lane == 0) atomicOr(a.err, kErrRounds);
             break;
@@ -740,7 +743,11 @@ __global__ void __launch_bounds__(BLOCK) k_sssp_nf(PathArgs a) {
     for (int v = threadIdx.x; v < n1; v += BLOCK) out[v] = DT<T>::val(dist[v]);
     if (a.stats) {
       for (int o = 16; o >= 1; o >>= 1) expanded += __shfl_down_sync(kFull, expanded, o);
-      if (lane == 0) atomicAdd(a.stats + 2, static_cast<unsigned long long>(expanded));
+      if (lane == 0) {
+        atomicAdd(a.stats + 2, static_cast<unsigned long long>(expanded));
+        atomicAdd(a.stats + 3, polls);
+        atomicAdd(a.stats + 4, batches);
+      }
       if (threadIdx.x == 0) {
         atomicAdd(a.stats + 0, static_cast<unsigned long long>(phases));
         atomicAdd(a.stats + 1, 1ull);

@@ -665,9 +665,9 @@ static int create_impl(const tapgpu_network* net, const tapgpu_demand* dem,
   TG_TRY(c->alloc_n(&c->counters, 2));
   TG_TRY(c->alloc_n(&c->err, 1));
   TG_TRY(c->alloc_n(&c->err_info, 2));
-  TG_TRY(c->alloc_n(&c->path_stats, 4));
+  TG_TRY(c->alloc_n(&c->path_stats, 8));
   TG_CUDA(cudaMemset(c->err, 0, sizeof(int)));
-  TG_CUDA(cudaMemset(c->path_stats, 0, 4 * sizeof(unsigned long long)));
+  TG_CUDA(cudaMemset(c->path_stats, 0, 8 * sizeof(unsigned long long)));
 
   // shortest-path label scratch between the two path kernels
   const size_t tb = static_cast<size_t>(n1) * (c->fp64 ? 8 : 4);
@@ -1183,7 +1183,7 @@ int tapgpu_set_timing(tapgpu_ctx* ctx, int on) {
     c->kt_n[i] = 0;
   }
   c->launches = 0;
-  TG_CUDA(cudaMemset(c->path_stats, 0, 4 * sizeof(unsigned long long)));
+  TG_CUDA(cudaMemset(c->path_stats, 0, 8 * sizeof(unsigned long long)));
   return TAPGPU_OK;
 }
 
@@ -1192,9 +1192,9 @@ int tapgpu_get_path_stats(tapgpu_ctx* ctx, int64_t* out) {
   Ctx* c = ctx->c;
   TG_CUDA(cudaSetDevice(c->device));
   TG_CUDA(cudaStreamSynchronize(c->stream));
-  unsigned long long v[4];
+  unsigned long long v[5];
   TG_CUDA(cudaMemcpy(v, c->path_stats, sizeof(v), cudaMemcpyDeviceToHost));
-  for (int i = 0; i < 4; ++i) out[i] = static_cast<int64_t>(v[i]);
+  for (int i = 0; i < 5; ++i) out[i] = static_cast<int64_t>(v[i]);
   return TAPGPU_OK;
 }
 

@@ -76,7 +76,7 @@ struct Ctx {
   int* err = nullptr;       // [1]
   int* err_info = nullptr;  // [2]
   int* pred_buf = nullptr;  // [dist_tasks][n1] for the shortest-path API
-  unsigned long long* path_stats = nullptr;  // [4] rounds, tasks, expansions (timing on)
+  unsigned long long* path_stats = nullptr;  // [8] rounds, tasks, expansions, idle polls, batches
   // buffers of the one-shot API (weights in both precisions, loaded volumes)
   uint2* api_e32 = nullptr;
   uint2* api_r32 = nullptr;

@@ -218,11 +218,13 @@ class Solver:
         out = {f"{k}_ms": float(ms[i]) for i, k in enumerate(names)}
         out.update({f"{k}_launches": int(n[i]) for i, k in enumerate(names)})
         out["kernel_launches"] = int(kl[0])
-        st = np.zeros(4, np.int64)
+        st = np.zeros(5, np.int64)
         K.check(self.L.tapgpu_get_path_stats(self.h, K.ptr(st, K.I64P)))
         out["sssp_rounds"] = int(st[0])
         out["sssp_tasks"] = int(st[1])
         out["sssp_expansions"] = int(st[2])
+        out["sssp_idle_polls"] = int(st[3])
+        out["sssp_batches"] = int(st[4])
         return out
 
     def profile_iteration(self, reps: int = 5) -> Dict[str, float]:
