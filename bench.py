@@ -82,6 +82,18 @@ class Dist:
             self.td.destroy_process_group()
 
 
+def shard_scenarios(net, count, rank):
+    """The upgrade scenarios of one rank: each rank draws its own set from a
+    rank-specific seed (scenarios are independent; nothing is exchanged)."""
+    from traffic_assignment_gb300 import synth
+    return synth.make_scenarios(net, count, seed=1004 + 7919 * rank)
+
+
+def whole_job_rate(dist, units, seconds):
+    """Units processed by all ranks / the slowest rank's time."""
+    return dist.sum(units) / dist.max(seconds)
+
+
 class ClockSampler:
     """nvidia-smi samples of SM clock and throttle reasons during a region."""
 
@@ -224,7 +236,7 @@ def run_ours(args, rank, world, local_rank):
     net, dem = synth.make_grid10k()
     S = args.scenarios
     # each rank solves its own scenario set (weak scaling: no data exchange)
-    scen = synth.make_scenarios(net, S, seed=1004 + 7919 * rank)
+    scen = shard_scenarios(net, S, rank)
     solver = Solver(net, dem, precision="fp32", device=local_rank)
 
     # base equilibrium: the warm start of every scenario
@@ -253,9 +265,8 @@ def run_ours(args, rank, world, local_rank):
     t0 = time.perf_counter()
     res = solver.solve_scenarios(scen, target_relgap=1e-4, max_iters=args.max_iters, x0=xb)
     torch.cuda.synchronize()
-    batched_s = dist.max(time.perf_counter() - t0)
     batched_iters = [q["iterations"] for q in res]
-    batched_sps = dist.sum(S) / batched_s
+    batched_sps = whole_job_rate(dist, S, time.perf_counter() - t0)
 
     # timed steps: batched FW iterations of all S scenarios (device timing)
     solver.run_iterations(args.warmup)
@@ -274,10 +285,11 @@ def run_ours(args, rank, world, local_rank):
         torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     dist.barrier()
-    ms = dist.max(ev0.elapsed_time(ev1))
+    ms_local = ev0.elapsed_time(ev1)
+    ms = dist.max(ms_local)
     tm = solver.timing()
     solver.set_timing(False)
-    value = dist.sum(S * args.steps) / (ms / 1e3)
+    value = whole_job_rate(dist, S * args.steps, ms_local / 1e3)
 
     # end to end through the C ABI from host buffers
     torch.cuda.synchronize()
@@ -285,8 +297,7 @@ def run_ours(args, rank, world, local_rank):
     t0 = time.perf_counter()
     res2 = solver.solve_scenarios(scen, max_iters=e2e_iters, x0=xb)
     outs = [solver.flows(s) for s in range(S)]
-    e2e_s = dist.max(time.perf_counter() - t0)
-    e2e_value = dist.sum(S * e2e_iters) / e2e_s
+    e2e_value = whole_job_rate(dist, S * e2e_iters, time.perf_counter() - t0)
     m = net.num_links
     n_edits = sum(len(sc.links) for sc in scen)
     h2d = S * m * 8 * 2 + n_edits * 16 + (S + 1) * 8 + m * 8

@@ -176,3 +176,40 @@ def test_screen_upgrades_first_order(built_lib, grid416):
         dv = oracle.replay_vht(net, cap, x0, Y)[0] - v0
         assert e < 0 and dv < 0
         assert abs(dv - e) <= 0.02 * abs(e)
+
+
+def test_adjoint_grid10k_random_links(built_lib):
+    """The 10,000-node network, 50 FW iterations with FP32 paths, 64 random
+    loaded links: central differences with a 1%-of-capacity step within 1e-3
+    relative (links whose gradient is below 1e-3 of the largest are held to
+    1e-6 of the largest instead: there the VHT's own rounding dominates)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    net, dem = synth.make_grid10k()
+    iters = 50
+    with _solve(net, dem, "fp32", iters=iters) as s:
+        v, g = s.adjoint_vht()
+        x0, D, lam, Y = _tape(s, iters)
+        x_end, _ = s.flows()
+    g_cpu = oracle.adjoint_vht(net, net.capacity, x0, D, lam)
+    gmax = np.abs(g_cpu).max()
+    np.testing.assert_allclose(g, g_cpu, rtol=0, atol=1e-9 * gmax)
+    rng = np.random.default_rng(2024)
+    links = rng.choice(np.flatnonzero(x_end > 0), 64, replace=False)
+    cap = net.capacity
+
+    def f(args):
+        a, h = args
+        c = cap.copy()
+        c[a] += h
+        return oracle.replay_vht(net, c, x0, Y)[0]
+
+    jobs = [(a, sgn * 0.01 * cap[a]) for a in links for sgn in (1.0, -1.0)]
+    with ThreadPoolExecutor(max_workers=16) as ex:  # ctypes calls release the GIL
+        vals = list(ex.map(f, jobs))
+    for i, a in enumerate(links):
+        fd = (vals[2 * i] - vals[2 * i + 1]) / (0.02 * cap[a])
+        if abs(g[a]) >= 1e-3 * gmax:
+            assert abs(fd - g[a]) <= 1e-3 * abs(g[a]), (a, fd, g[a])
+        else:
+            assert abs(fd - g[a]) <= 1e-6 * gmax, (a, fd, g[a])

@@ -270,7 +270,7 @@ int Ctx::plan_launches() {
                      ? opt.sssp_variant
                      : kSsspNearFar;
   sssp_block = opt.sssp_block > 0 ? opt.sssp_block : (sssp_variant == kSsspNearFar ? 256 : 512);
-  aon_block = opt.aon_block > 0 ? opt.aon_block : 512;
+  aon_block = opt.aon_block > 0 ? opt.aon_block : 1024;
   // leave room for the kernels' static shared memory (a few words)
   const size_t room = optin > 1024 ? static_cast<size_t>(optin - 1024) : 0;
   sssp_smem = sssp_smem_bytes(n1, fp64) <= room && !opt.global_scratch;
