@@ -337,6 +337,18 @@ int tapgpu_adjoint_vht(tapgpu_ctx *ctx, int scenario, double *grad, double *vht)
 int tapgpu_get_tape(tapgpu_ctx *ctx, int scenario, int iteration, double *x_checkpoint,
                     double *direction, double *lambda);
 
+/* Demand scenarios (trip modifications as a batched scenario axis): from the
+ * next tapgpu_solve_scenarios call with num_scen scenarios on, scenario s
+ * loads demand[s * nnz + i] for OD entry i, where the entries are those of
+ * the demand given to tapgpu_create in its order (origins 1..Z, each
+ * origin's destinations as listed) and nnz their count.  Only entries with
+ * positive base demand may be positive (a multiplier of the base, as
+ * tap/tap_functions.c:521-598 applies them); zero removes a pair.  The
+ * fixed-point scale of all demand is lowered if a scenario's total needs
+ * it.  num_scen 0 or demand NULL returns to the one base demand; single
+ * solves (tapgpu_solve) always use the base demand. */
+int tapgpu_set_scenario_demand(tapgpu_ctx *ctx, int num_scen, const double *demand);
+
 /* Shortest-path work counters gathered while timing is on (out has 5
  * entries): out[0] label correction rounds or near-far phases, out[1]
  * (scenario, origin) tasks, out[2] node expansions, and for the near-far

@@ -84,3 +84,66 @@ def test_farm_modes_from_net_mods_file(built_lib, tmp_path):
     subsets = scenarios.solve_farm(net, dem, path, "subsets", target_relgap=0, max_iters=5,
                                    warm_start=False, precision="fp32")
     assert len(subsets) == 5  # subsets of size >= 3 of 4 changes
+
+
+def _trip_sets(dem):
+    from traffic_assignment_gb300.tripmods import TripMod
+    z = dem.num_zones
+    return [[], [TripMod("p", "P2P", 2, 5, 3.0)], [TripMod("u", "UNIFORM", 4, 0, 0.5)],
+            [TripMod("d", "UNIFORM", 0, z - 1, 1.7), TripMod("a", "ALL", 0, 0, 1.2)],
+            [TripMod("z", "P2P", 1, 3, 0.0)]]
+
+
+@pytest.mark.parametrize("with_caps", [False, True])
+def test_trip_mod_demand_scenarios_match_oracle(built_lib, with_caps):
+    """Trip modifications as batched demand scenarios (FP64 paths), optionally
+    combined with capacity upgrades: each scenario against the oracle solving
+    the modified demand (1e-6), average excess cost on its own demand total."""
+    from traffic_assignment_gb300 import tripmods
+
+    net, dem = synth.make_grid416()
+    sets = _trip_sets(dem)
+    D = tripmods.demand_scenarios(dem, sets)
+    if with_caps:
+        scen = synth.make_scenarios(net, len(sets), seed=21)
+    else:
+        scen = [synth.Scenario(f"t{i}", np.zeros(0, np.int64), np.zeros(0))
+                for i in range(len(sets))]
+    with Solver(net, dem, precision="fp64") as s:
+        s.set_scenario_demand(D)
+        res = s.solve_scenarios(scen, max_iters=30)
+        flows = [s.flows(i)[0] for i in range(len(sets))]
+        traces = [s.trace(i) for i in range(len(sets))]
+        # back to the base demand: scenario 0 of a new batch is the base solve
+        s.set_scenario_demand(None)
+        s.solve_scenarios(scen[:1], max_iters=30)
+        base_again = s.flows(0)[0]
+    for i, ms in enumerate(sets):
+        cap = net.capacity.copy()
+        cap[scen[i].links] = scen[i].new_capacity
+        ref = oracle.frankwolfe(net, tripmods.apply_trip_mods(dem, ms), threads=1, max_iters=30,
+                                capacity=cap)
+        assert res[i]["error_bits"] == 0
+        assert _rel(flows[i], ref["x"]) < 1e-6, i
+        assert abs(res[i]["total_cost"] - ref["total_cost"]) <= 1e-6 * ref["total_cost"]
+        np.testing.assert_allclose(traces[i][:, 2], ref["trace"][:, 2], rtol=1e-6, atol=1e-9)
+    if not with_caps:
+        np.testing.assert_array_equal(flows[0], base_again)
+
+
+def test_demand_scenarios_argument_checks(built_lib):
+    net, dem = synth.make_small24()
+    with Solver(net, dem) as s:
+        D = np.tile(dem.od_demand[dem.od_ptr[1]:dem.od_ptr[dem.num_zones + 1]], (3, 1))
+        s.set_scenario_demand(D)
+        with pytest.raises(RuntimeError, match="demand scenarios were set for 3"):
+            s.solve_scenarios(synth.make_scenarios(net, 2), max_iters=3)
+        bad = D.copy()
+        bad[1, 0] = np.nan
+        with pytest.raises(RuntimeError, match="finite"):
+            s.set_scenario_demand(bad)
+        # single solves keep the base demand whatever is set
+        s.set_scenario_demand(D * 2.0)
+        r = s.solve(max_iters=5)
+        ref = oracle.frankwolfe(net, dem, threads=1, max_iters=5)
+        assert _rel(s.flows()[0], ref["x"]) < 1e-6 and r["iterations"] == 5

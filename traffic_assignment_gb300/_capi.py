@@ -81,7 +81,7 @@ EXPORTED = [
     "tapgpu_solve_scenarios", "tapgpu_sssp", "tapgpu_aon", "tapgpu_stream",
     "tapgpu_profile_iteration", "tapgpu_run_iterations", "tapgpu_set_timing",
     "tapgpu_get_timing", "tapgpu_get_path_stats", "tapgpu_sssp_labels_noalloc",
-    "tapgpu_adjoint_vht", "tapgpu_get_tape",
+    "tapgpu_adjoint_vht", "tapgpu_get_tape", "tapgpu_set_scenario_demand",
 ]
 EXPORTED_DATA = ["num_cores", "num_threads", "using_fermi_architecture"]
 
@@ -137,6 +137,8 @@ def load(path: str | None = None):
     L.tapgpu_adjoint_vht.restype = C.c_int
     L.tapgpu_get_tape.argtypes = [vp, C.c_int, C.c_int, F64P, F64P, F64P]
     L.tapgpu_get_tape.restype = C.c_int
+    L.tapgpu_set_scenario_demand.argtypes = [vp, C.c_int, F64P]
+    L.tapgpu_set_scenario_demand.restype = C.c_int
     for fn in ("tapgpu_create", "tapgpu_solve", "tapgpu_solve_begin", "tapgpu_solve_advance",
                "tapgpu_get_link_flows", "tapgpu_get_trace", "tapgpu_set_capacity",
                "tapgpu_solve_scenarios", "tapgpu_sssp", "tapgpu_aon",

@@ -878,7 +878,9 @@ __global__ void __launch_bounds__(BLOCK) k_aon(PathArgs a) {
     for (int j = __ldg(a.dem.od_ptr + sidx) + threadIdx.x; j < j1; j += BLOCK) {
       const int dest = __ldg(a.dem.od_dest + j);
       if (dest == src || !(__ldg(a.dem.od_dem + j) > 0.0)) continue;
-      const unsigned long long q = static_cast<unsigned long long>(__ldg(a.dem.od_q + j));
+      const unsigned long long q =
+          static_cast<unsigned long long>(__ldg(a.dem.od_q + scen * a.dem.q_stride + j));
+      if (q == 0 && a.dem.q_stride) continue;  // a demand scenario removed this OD pair
       if (dest < 0 || dest >= n1 || parent[dest] < 0) {
         atomicOr(a.err, kErrNoPath);
         a.err_info[0] = src;
@@ -1147,7 +1149,8 @@ __global__ void __launch_bounds__(kLinkBlock) k_ls_pass(LinkArgs a) {
     for (unsigned b = 0; b < gridDim.x; ++b)
       for (int i = 0; i < kNumSums; ++i)
         tot[i] = __dadd_rn(tot[i], vload(p0 + b * kNumSums + i));
-    ls_decide(st, tot, e0, a.pass, a.total_demand, a.ls_mode);
+    ls_decide(st, tot, e0, a.pass, a.total_demand_s ? a.total_demand_s[scen] : a.total_demand,
+              a.ls_mode);
     a.arrive[scen] = 0u;
   }
 }

@@ -70,6 +70,7 @@ struct Demand {
   const int* od_ptr;            // [num_sources+1]
   const int* od_dest;           // destination node
   const long long* od_q;        // demand in fixed point (2^-scale_bits units)
+  long long q_stride;           // entries per scenario in od_q (0: one demand for all)
   const double* od_dem;         // demand as given (for the no-path check)
   double inv_scale;             // 2^-scale_bits
   double total;                 // total demand (tap/tap_functions.c:377-386)
@@ -126,6 +127,7 @@ struct LinkArgs {
   int trace_cap;
   double inv_scale;             // fixed point -> volume
   double total_demand;
+  const double* total_demand_s; // [S] per-scenario totals (demand scenarios) or null
   int pass;                     // line-search pass index
   int* err;
   double* x_hist;               // [S][hist_cap / ckpt_every + 1][m] flows at checkpoints

@@ -136,7 +136,8 @@ Demand Ctx::demand() const {
   Demand dm;
   dm.od_ptr = od_ptr;
   dm.od_dest = od_dest;
-  dm.od_q = od_q;
+  dm.od_q = use_dem_scen ? sc_od_q : od_q;
+  dm.q_stride = use_dem_scen ? nnz : 0;
   dm.od_dem = od_dem;
   dm.inv_scale = inv_scale;
   dm.total = total_demand;
@@ -194,6 +195,7 @@ LinkArgs Ctx::link_args(int nscen) const {
   a.trace_cap = trace_cap;
   a.inv_scale = inv_scale;
   a.total_demand = total_demand;
+  a.total_demand_s = use_dem_scen ? sc_total : nullptr;
   a.err = err;
   a.x_hist = x_hist;
   a.d_hist = d_hist;
@@ -310,6 +312,8 @@ int Ctx::enqueue_paths(int nscen, bool load, const uint2* e32p, const uint2* r32
     if (!use_state) {
       a.state = nullptr;
       a.scen_list = nullptr;
+      a.dem.od_q = od_q;
+      a.dem.q_stride = 0;
     }
     const int ntask = static_cast<int>(t1 - t0);
     a.scratch_stride = static_cast<long long>(sssp_smem_bytes(n1, fp64));
@@ -386,7 +390,7 @@ int Ctx::run_graph(int iters, int nscen) {
     }
     return TAPGPU_OK;
   }
-  if (!gexec || g_iters != iters || g_nscen != nscen) {
+  if (!gexec || g_iters != iters || g_nscen != nscen || g_dem != use_dem_scen) {
     if (gexec) {
       cudaGraphExecDestroy(gexec);
       gexec = nullptr;
@@ -416,6 +420,7 @@ int Ctx::run_graph(int iters, int nscen) {
     }
     g_iters = iters;
     g_nscen = nscen;
+    g_dem = use_dem_scen;
   }
   TG_CUDA(cudaGraphLaunch(gexec, stream));
   launches += g_kernels;
@@ -643,6 +648,8 @@ static int create_impl(const tapgpu_network* net, const tapgpu_demand* dem,
   }
   c->inv_scale = std::ldexp(1.0, -c->scale_bits);
   c->total_demand = total;
+  c->h_od_dem = odem;
+  c->nnz = static_cast<long long>(odem.size());
   std::vector<int> src(std::max(Z, 1));
   for (int i = 0; i < Z; ++i) src[i] = i + 1;
   TG_TRY(c->alloc_n(&c->od_ptr, Z + 1));
@@ -812,6 +819,7 @@ int tapgpu_solve_begin(tapgpu_ctx* ctx, int max_iters, double target_relgap, con
   Ctx* c = ctx->c;
   TG_CUDA(cudaSetDevice(c->device));
   TG_TRY(c->ensure_scenarios(1));
+  c->use_dem_scen = false;
   TG_CUDA(cudaMemcpy(c->cap, c->h_cap.data(), sizeof(double) * c->M, cudaMemcpyHostToDevice));
   std::vector<int> one{0};
   TG_CUDA(cudaMemcpyAsync(c->scen_list, one.data(), sizeof(int), cudaMemcpyHostToDevice, c->stream));
@@ -918,8 +926,14 @@ int tapgpu_solve_scenarios(tapgpu_ctx* ctx, int num_scen, const int64_t* scen_pt
         return TAPGPU_ERR_ARG;
       }
   }
+  if (c->dem_scen && c->dem_scen != num_scen) {
+    tapgpu::set_message("demand scenarios were set for " + std::to_string(c->dem_scen) +
+                        " scenarios, not " + std::to_string(num_scen));
+    return TAPGPU_ERR_ARG;
+  }
   TG_CUDA(cudaSetDevice(c->device));
   TG_TRY(c->ensure_scenarios(num_scen));
+  c->use_dem_scen = c->dem_scen == num_scen;
   c->last_nscen = num_scen;
   // capacities of every scenario: base with the scenario's edits
   std::vector<double> caps(static_cast<size_t>(num_scen) * M);
@@ -952,6 +966,13 @@ int tapgpu_solve_scenarios(tapgpu_ctx* ctx, int num_scen, const int64_t* scen_pt
                               cudaMemcpyHostToDevice, c->stream));
     TG_CUDA(cudaStreamSynchronize(c->stream));
     TG_TRY(c->enqueue_initial(num_scen, true));
+  } else if (c->use_dem_scen) {
+    // every scenario has its own demand: load each at free flow
+    tapgpu::LinkArgs la = c->link_args(num_scen);
+    TG_CUDA(tapgpu::launch_set_costs(la, c->link_grid, c->stream));
+    TG_TRY(c->enqueue_paths(num_scen, true, c->e32, c->r32, c->w64, c->yfx, true));
+    la.pass = 0;
+    TG_CUDA(tapgpu::launch_init_flows(la, c->link_grid, c->stream));
   } else {
     // free-flow all-or-nothing does not depend on capacity: load scenario 0
     // once and start every scenario from it
@@ -973,6 +994,71 @@ int tapgpu_solve_scenarios(tapgpu_ctx* ctx, int num_scen, const int64_t* scen_pt
   TG_CUDA(cudaMemcpy(&e, c->err, sizeof(int), cudaMemcpyDeviceToHost));
   if (results)
     for (int s = 0; s < num_scen; ++s) tapgpu::fill_result(st[s], e, &results[s]);
+  return TAPGPU_OK;
+}
+
+int tapgpu_set_scenario_demand(tapgpu_ctx* ctx, int num_scen, const double* demand) {
+  if (!ctx || num_scen < 0) return TAPGPU_ERR_ARG;
+  Ctx* c = ctx->c;
+  TG_CUDA(cudaSetDevice(c->device));
+  TG_CUDA(cudaStreamSynchronize(c->stream));
+  if (c->sc_od_q) tapgpu::free_owned(c, c->sc_od_q);
+  if (c->sc_total) tapgpu::free_owned(c, c->sc_total);
+  c->sc_od_q = nullptr;
+  c->sc_total = nullptr;
+  c->dem_scen = 0;
+  c->use_dem_scen = false;
+  if (c->gexec) {  // captured launches hold the old demand pointers
+    cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+  }
+  c->g_nscen = -1;
+  if (num_scen == 0 || !demand) return TAPGPU_OK;
+  const long long nnz = c->nnz;
+  if (nnz == 0) {
+    tapgpu::set_message("the context has no demand to vary");
+    return TAPGPU_ERR_ARG;
+  }
+  std::vector<double> totals(num_scen);
+  double max_pos = 0.0;
+  for (int s = 0; s < num_scen; ++s) {
+    double tot = 0.0, pos = 0.0;
+    for (long long i = 0; i < nnz; ++i) {
+      const double v = demand[static_cast<size_t>(s) * nnz + i];
+      if (std::isnan(v) || std::isinf(v)) {
+        tapgpu::set_message("scenario demand must be finite");
+        return TAPGPU_ERR_ARG;
+      }
+      if (v > 0 && !(c->h_od_dem[i] > 0)) {
+        tapgpu::set_message("a demand scenario can only change OD pairs with positive base demand");
+        return TAPGPU_ERR_ARG;
+      }
+      tot += v;  // tap/tap_functions.c:377-386 sums every entry
+      if (v > 0) pos += v;
+    }
+    totals[s] = tot;
+    max_pos = std::max(max_pos, pos);
+  }
+  // keep every node/link total below 2^61 in the shared fixed point
+  int bits = 40;
+  if (max_pos > 1.0) bits = std::min(40, 61 - static_cast<int>(std::ceil(std::log2(max_pos))) - 1);
+  if (bits < c->scale_bits) {
+    const double scale = std::ldexp(1.0, bits);
+    std::vector<long long> oq(nnz);
+    for (long long i = 0; i < nnz; ++i)
+      oq[i] = c->h_od_dem[i] > 0 ? std::llrint(c->h_od_dem[i] * scale) : 0;
+    TG_CUDA(cudaMemcpy(c->od_q, oq.data(), sizeof(long long) * nnz, cudaMemcpyHostToDevice));
+    c->scale_bits = bits;
+    c->inv_scale = std::ldexp(1.0, -bits);
+  }
+  const double scale = std::ldexp(1.0, c->scale_bits);
+  std::vector<long long> q(static_cast<size_t>(num_scen) * nnz);
+  for (size_t i = 0; i < q.size(); ++i) q[i] = demand[i] > 0 ? std::llrint(demand[i] * scale) : 0;
+  TG_TRY(c->alloc_n(&c->sc_od_q, q.size()));
+  TG_TRY(c->alloc_n(&c->sc_total, static_cast<size_t>(num_scen)));
+  TG_CUDA(cudaMemcpy(c->sc_od_q, q.data(), sizeof(long long) * q.size(), cudaMemcpyHostToDevice));
+  TG_CUDA(cudaMemcpy(c->sc_total, totals.data(), sizeof(double) * num_scen, cudaMemcpyHostToDevice));
+  c->dem_scen = num_scen;
   return TAPGPU_OK;
 }
 

@@ -41,6 +41,13 @@ struct Ctx {
   int* sources = nullptr;
   double inv_scale = 1.0, total_demand = 0.0;
   int scale_bits = 0;
+  // demand scenarios (trip modifications): their own OD demand per scenario
+  std::vector<double> h_od_dem;  // base demand in device entry order
+  long long nnz = 0;
+  long long* sc_od_q = nullptr;  // [dem_scen][nnz] fixed point
+  double* sc_total = nullptr;    // [dem_scen] demand totals
+  int dem_scen = 0;              // scenarios with their own demand (0: none set)
+  bool use_dem_scen = false;     // the current batched solve uses them
 
   // per-scenario state (capacity for S_cap scenarios)
   int S_cap = 0;
@@ -86,6 +93,7 @@ struct Ctx {
   cudaStream_t stream = nullptr;
   cudaGraphExec_t gexec = nullptr;
   int g_iters = 0, g_nscen = -1;
+  bool g_dem = false;
   int solve_max_iters = 0;
   int last_nscen = 1;  // scenarios of the last solve (for run_iterations)
 

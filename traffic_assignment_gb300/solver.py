@@ -162,6 +162,18 @@ class Solver:
         K.check(self.L.tapgpu_aon(self.h, K.ptr(w, K.F64P), K.ptr(y, K.F64P)))
         return y
 
+    def set_scenario_demand(self, demand: Optional[np.ndarray]):
+        """Per-scenario OD demand [S][nnz] (entries in the order of the Demand
+        given at construction) for the following solve_scenarios calls; None
+        returns to the base demand."""
+        if demand is None:
+            K.check(self.L.tapgpu_set_scenario_demand(self.h, 0, None))
+            return
+        da = np.ascontiguousarray(demand, np.float64)
+        if da.ndim != 2:
+            raise ValueError("demand must be [scenarios][OD entries]")
+        K.check(self.L.tapgpu_set_scenario_demand(self.h, da.shape[0], K.ptr(da, K.F64P)))
+
     def solve_scenarios(self, scenarios: List[Scenario], max_iters: int = 0,
                         target_relgap: float = 0.0, x0: Optional[np.ndarray] = None):
         ptr = [0]
