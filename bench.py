@@ -345,7 +345,7 @@ def run_ours(args, rank, world, local_rank):
                                     for k in ("sssp", "aon", "line_search", "step")},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "k_sssp_nf", "peak_kind": f"{peak_kind} hbm_gbs",
+                         "kernel": "k_sssp_nfq", "peak_kind": f"{peak_kind} hbm_gbs",
                          "algorithmic_bytes_per_launch": bytes_per_launch,
                          "tasks_per_launch": tasks_per_launch,
                          "avg_launch_ms": sssp_avg_ms,

@@ -236,9 +236,12 @@ typedef struct tapgpu_options_s {
   int record_tape;       /* keep per-iteration flows and directions for the adjoint */
   int tape_capacity;     /* iterations kept on the tape */
   int global_scratch;    /* 1: per-CTA labels in global memory even when shared memory fits */
-  int sssp_variant;      /* 0 default; 1 bulk-synchronous rounds; 2 asynchronous warp-owned
-                            frontier; 3 asynchronous near set below a rising threshold */
-  double nf_delta;       /* threshold step of variant 3 in cost units; 0 = 16 x mean link cost */
+  int sssp_variant;      /* 0 default (4, or 3 above 65535 nodes); 1 bulk-synchronous
+                            rounds; 2 asynchronous warp-owned frontier; 3 asynchronous near
+                            set below a rising threshold; 4 as 3 with a FIFO ring of near
+                            nodes (networks of at most 65535 nodes) */
+  double nf_delta;       /* threshold step of variants 3 and 4 in cost units; 0 = 16 x mean
+                            link cost */
   int line_search;       /* 0: the reference's 2^-k rule; 1: exact root of the directional
                             derivative (differentiable step sizes, for the adjoint) */
   int tape_checkpoint;   /* with record_tape: flows kept every this many iterations and
@@ -349,11 +352,12 @@ int tapgpu_get_tape(tapgpu_ctx *ctx, int scenario, int iteration, double *x_chec
  * solves (tapgpu_solve) always use the base demand. */
 int tapgpu_set_scenario_demand(tapgpu_ctx *ctx, int num_scen, const double *demand);
 
-/* Shortest-path work counters gathered while timing is on (out has 5
+/* Shortest-path work counters gathered while timing is on (out has 6
  * entries): out[0] label correction rounds or near-far phases, out[1]
  * (scenario, origin) tasks, out[2] node expansions, and for the near-far
- * kernel out[3] idle polls of warps that found no near work and out[4]
- * warp batches of up to 32 expansions. */
+ * kernels out[3] idle polls of warps that found no near work, out[4] warp
+ * batches of up to 32 expansions and out[5] (queue variant) nodes claimed by
+ * the bitmap word scan instead of the ring. */
 int tapgpu_get_path_stats(tapgpu_ctx *ctx, int64_t *out);
 
 /* No counterpart in the reference.  All-origins FP64 shortest-path labels for

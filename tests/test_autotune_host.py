@@ -8,12 +8,12 @@ from traffic_assignment_gb300 import synth
 
 def test_candidates_cover_every_variant_and_block():
     c = A.candidates()
-    assert {x.sssp_variant for x in c} == {"rounds", "async", "nearfar"}
+    assert {x.sssp_variant for x in c} == {"rounds", "async", "nearfar", "nearfar_queue"}
     assert {x.sssp_block for x in c} == {128, 256, 512, 1024}
     assert {x.aon_block for x in c} == {256, 512, 1024}
     assert len(set(c)) == len(c)
     q = A.candidates(quick=True)
-    assert set(q) <= set(c) | {A.Candidate("nearfar", 256, 16.0, a) for a in (256, 1024)}
+    assert set(q) <= set(c)
 
 
 def test_solver_kwargs():

@@ -14,7 +14,8 @@ def test_tune_and_cache(built_lib, tmp_path):
     net, dem = synth.make_grid416()
     cache = str(tmp_path / "tune.json")
     cands = [A.Candidate("rounds", 512), A.Candidate("async", 256),
-             A.Candidate("nearfar", 256, 16.0), A.Candidate("nearfar", 128, 4.0, 256)]
+             A.Candidate("nearfar", 256, 16.0), A.Candidate("nearfar_queue", 256, 16.0),
+             A.Candidate("nearfar_queue", 128, 4.0, 256)]
     r = A.tune(net, dem, "fp32", scenarios=8, iters=2, warm_iters=10, cache=cache, cands=cands)
     assert not r.from_cache
     assert len(r.table) == len(cands)

@@ -4,7 +4,7 @@ The fastest shortest-path kernel depends on the network (node count, degree,
 cost spread) and on how many tasks a launch holds.  ``tune`` sweeps
 
   * the shortest-path variant: bulk-synchronous rounds, asynchronous
-    worklist, near-far (the default),
+    worklist, near-far, near-far with a FIFO ring (the default),
   * its block size (128 .. 1024 threads),
   * the near-far phase step, as a multiple of the mean free-flow time,
   * the all-or-nothing loading block size,
@@ -35,20 +35,20 @@ from .synth import Demand, Network, make_scenarios
 
 __all__ = ["Candidate", "TuneResult", "candidates", "tune", "tuned_options", "cache_key"]
 
-_VARIANTS = ("rounds", "async", "nearfar")
+_VARIANTS = ("rounds", "async", "nearfar", "nearfar_queue")
 
 
 @dataclass(frozen=True)
 class Candidate:
-    sssp_variant: str = "nearfar"
+    sssp_variant: str = "nearfar_queue"
     sssp_block: int = 256
     nf_scale: float = 16.0  # near-far step = nf_scale x mean free-flow time
-    aon_block: int = 512
+    aon_block: int = 1024
 
     def solver_kwargs(self, net: Network) -> Dict:
         kw = dict(sssp_variant=self.sssp_variant, sssp_block=self.sssp_block,
                   aon_block=self.aon_block)
-        if self.sssp_variant == "nearfar":
+        if self.sssp_variant.startswith("nearfar"):
             kw["nf_delta"] = float(self.nf_scale * np.mean(net.fft))
         return kw
 
@@ -72,12 +72,12 @@ def candidates(quick: bool = False) -> List[Candidate]:
     scales = (8.0, 16.0, 32.0) if quick else (4.0, 8.0, 16.0, 32.0, 64.0)
     for v in _VARIANTS:
         for b in blocks:
-            if v == "nearfar":
-                out.extend(Candidate(v, b, s, 512) for s in scales)
+            if v.startswith("nearfar"):
+                out.extend(Candidate(v, b, s, 1024) for s in scales)
             else:
-                out.append(Candidate(v, b, 16.0, 512))
+                out.append(Candidate(v, b, 16.0, 1024))
     # the loading kernel's block, at the default shortest-path shape
-    out.extend(Candidate("nearfar", 256, 16.0, a) for a in (256, 1024))
+    out.extend(Candidate("nearfar_queue", 256, 16.0, a) for a in (256, 512))
     return out
 
 

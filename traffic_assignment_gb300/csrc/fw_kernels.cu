@@ -756,6 +756,366 @@ __global__ void __launch_bounds__(BLOCK) k_sssp_nf(PathArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Near-far with a FIFO of near nodes (k_sssp_nfq)
+// ---------------------------------------------------------------------------
+// The near bitmap stays the record of which nodes wait for expansion (a set
+// bit is a pending node, as in k_sssp_nf); a ring of 16-bit node ids in
+// shared memory lists them in push order so that a warp takes 32 at once
+// with one compare-and-swap instead of scanning its bitmap words.  A node is
+// expanded by whoever clears its bit (atomicAnd / atomicExch), so stale ring
+// entries are skipped, and a node that finds the ring full waits in the
+// bitmap, where the word scan of k_sssp_nf still finds it.  The ring is an
+// accelerator only: losing an entry cannot lose a node.
+constexpr int kQCap = kQueueSlots;           // ring slots
+constexpr unsigned short kQEmpty = 0xffffu;  // a free slot (node ids are < 0xffff)
+constexpr int kMaxSlotSpins = 1 << 20;       // bound on waiting for one slot
+
+// Append v to the ring unless fewer than BLOCK slots are free (one per
+// thread that may be appending at the same time, so no append overruns a
+// slot whose previous node has been claimed but not yet read).
+template <int BLOCK>
+__device__ __forceinline__ void ring_push(unsigned short* ring, unsigned* qhead, unsigned* qtail,
+                                          int v, int* err) {
+  if constexpr (BLOCK >= kQCap) {
+    return;  // no room for a margin of one slot per thread: the bitmap alone
+  } else {
+    if (vload(qtail) - vload(qhead) >= static_cast<unsigned>(kQCap - BLOCK)) return;
+    const unsigned pos = atomicAdd(qtail, 1u);
+    volatile unsigned short* slot = ring + (pos & (kQCap - 1));
+    int spins = 0;
+    while (*slot != kQEmpty) {  // the previous lap's node is being read right now
+      if (++spins > kMaxSlotSpins) {
+        atomicOr(err, kErrRounds);
+        break;
+      }
+    }
+    *slot = static_cast<unsigned short>(v);
+  }
+}
+
+template <typename T, int BLOCK>
+__device__ __forceinline__ int relax_range_nfq(int src, int e0, int e1, int first_thru,
+                                               const Edges<T>& ed, typename DT<T>::U* dist,
+                                               unsigned* near, unsigned* far, T du,
+                                               typename DT<T>::U thr_bits, unsigned short* ring,
+                                               unsigned* qhead, unsigned* qtail, int* err) {
+  using U = typename DT<T>::U;
+  int pushes = 0;
+  for (int b = e0; b < e1; b += kEdgeGroup) {
+    int hh[kEdgeGroup];
+    T ww[kEdgeGroup];
+#pragma unroll
+    for (int j = 0; j < kEdgeGroup; ++j)
+      if (b + j < e1) ed.load(b + j, hh[j], ww[j]);
+#pragma unroll
+    for (int j = 0; j < kEdgeGroup; ++j) {
+      if (b + j >= e1) break;
+      const int h = hh[j];
+      const U nb = DT<T>::bits(DT<T>::add(du, ww[j]));
+      if (nb < vload(dist + h)) {
+        const U old = atomicMin(dist + h, nb);
+        if (nb < old && !(h < first_thru && h != src)) {
+          const unsigned bit = 1u << (h & 31);
+          if (nb < thr_bits) {
+            if (!(vload(near + (h >> 5)) & bit)) {
+              const unsigned prev = atomicOr(near + (h >> 5), bit);
+              if (!(prev & bit)) {
+                ++pushes;
+                ring_push<BLOCK>(ring, qhead, qtail, h, err);
+              }
+            }
+          } else if (!(vload(far + (h >> 5)) & bit)) {
+            atomicOr(far + (h >> 5), bit);
+          }
+        }
+      }
+    }
+  }
+  return pushes;
+}
+
+// Expand each lane's claimed node (valid) with the reservation protocol of
+// k_sssp_async: `pending` is raised by the out-degree before relaxing, so it
+// cannot reach zero while this warp may still push.
+template <typename T, int BLOCK>
+__device__ __forceinline__ void nfq_expand(const PathArgs& a, int src, int F, const Edges<T>& ed,
+                                           typename DT<T>::U* dist, unsigned* near,
+                                           unsigned* far, typename DT<T>::U thr,
+                                           unsigned short* ring, unsigned* qhead,
+                                           unsigned* qtail, int* pending, int v, bool valid,
+                                           unsigned& expanded) {
+  const int lane = threadIdx.x & 31;
+  int e0 = 0, e1 = 0;
+  if (valid && !(v < F && v != src)) {
+    e0 = __ldg(a.g.row_ptr + v);
+    e1 = __ldg(a.g.row_ptr + v + 1);
+  }
+  // out-degrees and claimed nodes in one sum (degrees < 2^25 per warp)
+  const int packed = warp_sum(((e1 - e0) << 6) | (valid ? 1 : 0));
+  const int reserve = packed >> 6, items = packed & 63;
+  if (lane == 0) {
+    atomicAdd(pending, reserve);
+    __threadfence_block();
+  }
+  __syncwarp();
+  int pushes = 0;
+  if (e1 > e0)
+    pushes = relax_range_nfq<T, BLOCK>(src, e0, e1, F, ed, dist, near, far,
+                                       DT<T>::val(vload(dist + v)), thr, ring, qhead, qtail,
+                                       a.err);
+  expanded += valid ? 1u : 0u;
+  const int used = warp_sum(pushes);
+  __syncwarp();
+  if (lane == 0) {
+    __threadfence_block();
+    atomicAdd(pending, -(reserve - used + items));
+  }
+}
+
+// five 256-thread CTAs per SM fit the shared memory of a 10k-node network:
+// keep registers to that occupancy
+template <typename T, int BLOCK, bool SMEM>
+__global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) k_sssp_nfq(PathArgs a) {
+  using U = typename DT<T>::U;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int sh_task;
+  __shared__ int pending;
+  __shared__ U sh_min;
+  __shared__ unsigned qhead, qtail;
+  const int n1 = a.g.n1;
+  const int nwords = (n1 + 31) >> 5;
+  unsigned char* base =
+      SMEM ? smem_raw
+           : static_cast<unsigned char*>(a.scratch) + static_cast<size_t>(blockIdx.x) * a.scratch_stride;
+  U* dist = reinterpret_cast<U*>(base);
+  unsigned* near = reinterpret_cast<unsigned*>(base + align16(sizeof(U) * n1));
+  unsigned* far = near + nwords;
+  unsigned short* ring = reinterpret_cast<unsigned short*>(far + nwords);
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  constexpr int kWarps = BLOCK / 32;
+  const int F = a.g.first_thru;
+  const int my_words = warp < nwords ? (nwords - warp + kWarps - 1) / kWarps : 0;
+  const T delta = static_cast<T>(a.nf_delta);
+
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) sh_task = atomicAdd(a.counter, 1) + a.task_begin;
+    __syncthreads();
+    const int task = sh_task;
+    if (task >= a.task_end) break;
+    const int slot = task / a.num_sources;
+    const int scen = a.scen_list ? a.scen_list[slot] : 0;
+    if (a.state && a.state[scen].done) continue;
+    const int src = a.sources[task - slot * a.num_sources];
+    const Edges<T> ed = edges_of<T>(a, scen);
+    unsigned expanded = 0;
+    unsigned long long polls = 0, batches = 0, scanned = 0;
+    int phases = 0;
+
+    for (int v = threadIdx.x; v < n1; v += BLOCK) dist[v] = DT<T>::kInf;
+    for (int i = threadIdx.x; i < 2 * nwords; i += BLOCK) near[i] = 0u;
+    for (int i = threadIdx.x; i < kQCap; i += BLOCK) ring[i] = kQEmpty;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      dist[src] = DT<T>::bits(T(0));
+      near[src >> 5] = 1u << (src & 31);
+      pending = 1;
+      ring[0] = static_cast<unsigned short>(src);
+      qhead = 0u;
+      qtail = 1u;
+    }
+    __syncthreads();
+    U thr = DT<T>::bits(delta);
+
+    for (;;) {  // phases
+      long long idle = 0;
+      for (;;) {
+        int claimed_any = 0;
+        // -- batches of up to 32 nodes from the ring ---------------------------
+        for (;;) {
+          unsigned h = 0u;
+          int n = 0;
+          if (lane == 0) {
+            for (int tries = 0; tries < 64; ++tries) {
+              h = vload(&qhead);
+              const int avail = static_cast<int>(vload(&qtail) - h);
+              if (avail <= 0) break;
+              const int take = avail < 32 ? avail : 32;
+              if (atomicCAS(&qhead, h, h + static_cast<unsigned>(take)) == h) {
+                n = take;
+                break;
+              }
+            }
+          }
+          n = __shfl_sync(kFull, n, 0);
+          if (n == 0) break;
+          h = __shfl_sync(kFull, h, 0);
+          claimed_any = 1;
+          int v = 0;
+          bool valid = false;
+          if (lane < n) {
+            volatile unsigned short* sl = ring + ((h + static_cast<unsigned>(lane)) & (kQCap - 1));
+            unsigned short q = *sl;
+            int spins = 0;
+            while (q == kQEmpty && ++spins <= kMaxSlotSpins) q = *sl;
+            if (q != kQEmpty) {
+              *sl = kQEmpty;
+              v = q;
+              const unsigned bit = 1u << (v & 31);
+              valid = (atomicAnd(near + (v >> 5), ~bit) & bit) != 0u;
+            } else {
+              atomicOr(a.err, kErrRounds);
+            }
+          }
+          ++batches;
+          nfq_expand<T, BLOCK>(a, src, F, ed, dist, near, far, thr, ring, &qhead, &qtail,
+                               &pending, v, valid, expanded);
+        }
+        // -- nodes that found the ring full: scan this warp's bitmap words ------
+        for (int j0 = 0; j0 < my_words; j0 += 32) {
+          const int j = j0 + lane;
+          const int wi = warp + j * kWarps;
+          unsigned word = 0u;
+          if (j < my_words) {
+            word = vload(near + wi);
+            if (word) word = atomicExch(near + wi, 0u);
+          }
+          const int cnt = __popc(word);
+          int incl = cnt;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(kFull, incl, o);
+            if (lane >= o) incl += y;
+          }
+          const int total = __shfl_sync(kFull, incl, 31);
+          if (total == 0) continue;
+          claimed_any = 1;
+          for (int b = 0; b < total; b += 32) {
+            const int jj = b + lane;
+            int owner = 0;
+#pragma unroll
+            for (int step = 16; step >= 1; step >>= 1) {
+              const int probe = __shfl_sync(kFull, incl, owner + step - 1);
+              if (probe <= jj) owner += step;
+            }
+            owner &= 31;
+            const unsigned ow = __shfl_sync(kFull, word, owner);
+            const int oincl = __shfl_sync(kFull, incl, owner);
+            const bool valid = jj < total;
+            int v = 0;
+            if (valid)
+              v = ((warp + (j0 + owner) * kWarps) << 5) + nth_set_bit(ow, jj - (oincl - __popc(ow)));
+            ++batches;
+            scanned += valid ? 1u : 0u;
+            nfq_expand<T, BLOCK>(a, src, F, ed, dist, near, far, thr, ring, &qhead, &qtail,
+                                 &pending, v, valid, expanded);
+          }
+        }
+        if (!claimed_any) {
+          if (vload(&pending) <= 0) break;
+          ++polls;
+          if (++idle > kMaxIdlePolls) {
+            if (lane == 0) atomicOr(a.err, kErrRounds);
+            break;
+          }
+          __nanosleep(32);
+        }
+      }
+      __syncthreads();
+      // -- phase step (as k_sssp_nf), promoted nodes also go to the ring ---------
+      int left = 0;
+      for (int i = threadIdx.x; i < nwords; i += BLOCK) left |= (near[i] != 0u);
+      if (__syncthreads_or(left)) {  // a warp left early: recount and resume
+        if (threadIdx.x == 0) pending = 0;
+        __syncthreads();
+        int c = 0;
+        for (int i = threadIdx.x; i < nwords; i += BLOCK) c += __popc(near[i]);
+        c = warp_sum(c);
+        if (lane == 0) atomicAdd(&pending, c);
+        __syncthreads();
+        if (++phases > a.max_rounds) {
+          if (threadIdx.x == 0) atomicOr(a.err, kErrRounds);
+          break;
+        }
+        continue;
+      }
+      if (threadIdx.x == 0) sh_min = DT<T>::kInf;
+      __syncthreads();
+      U mn = DT<T>::kInf;
+      for (int i = threadIdx.x; i < nwords; i += BLOCK) {
+        const unsigned w = far[i];
+        if (!w) continue;
+        unsigned keep = 0u, ww = w;
+        while (ww) {
+          const int bpos = __ffs(ww) - 1;
+          ww &= ww - 1;
+          const U dv = dist[(i << 5) + bpos];
+          if (dv >= thr) {
+            keep |= 1u << bpos;
+            if (dv < mn) mn = dv;
+          }
+        }
+        if (keep != w) far[i] = keep;
+      }
+      if (mn != DT<T>::kInf) atomicMin(&sh_min, mn);
+      __syncthreads();
+      const U fmin = sh_min;
+      if (fmin == DT<T>::kInf) break;  // nothing left: labels are final
+      thr = DT<T>::bits(DT<T>::add(DT<T>::val(fmin), delta));
+      if (thr <= fmin) thr = fmin + 1;
+      int moved = 0;
+      for (int i = threadIdx.x; i < nwords; i += BLOCK) {
+        const unsigned w = far[i];
+        if (!w) continue;
+        unsigned take = 0u;
+        unsigned ww = w;
+        while (ww) {
+          const int bpos = __ffs(ww) - 1;
+          ww &= ww - 1;
+          if (dist[(i << 5) + bpos] < thr) take |= 1u << bpos;
+        }
+        if (take) {
+          far[i] = w & ~take;
+          near[i] = take;
+          moved += __popc(take);
+          unsigned tt = take;
+          while (tt) {
+            const int bpos = __ffs(tt) - 1;
+            tt &= tt - 1;
+            ring_push<BLOCK>(ring, &qhead, &qtail, (i << 5) + bpos, a.err);
+          }
+        }
+      }
+      if (threadIdx.x == 0) pending = 0;
+      __syncthreads();
+      moved = warp_sum(moved);
+      if (lane == 0 && moved) atomicAdd(&pending, moved);
+      __syncthreads();
+      if (++phases > a.max_rounds) {
+        if (threadIdx.x == 0) atomicOr(a.err, kErrRounds);
+        break;
+      }
+    }
+    T* out = static_cast<T*>(a.dist) + static_cast<size_t>(task - a.task_begin) * n1;
+    for (int v = threadIdx.x; v < n1; v += BLOCK) out[v] = DT<T>::val(dist[v]);
+    if (a.stats) {
+      for (int o = 16; o >= 1; o >>= 1) expanded += __shfl_down_sync(kFull, expanded, o);
+      if (lane == 0) {
+        atomicAdd(a.stats + 2, static_cast<unsigned long long>(expanded));
+        atomicAdd(a.stats + 3, polls);
+        atomicAdd(a.stats + 4, batches);
+        atomicAdd(a.stats + 5, scanned);
+      }
+      if (threadIdx.x == 0) {
+        atomicAdd(a.stats + 0, static_cast<unsigned long long>(phases));
+        atomicAdd(a.stats + 1, 1ull);
+      }
+    }
+  }
+}
+
 template <typename T, int BLOCK, bool SMEM>
 __global__ void __launch_bounds__(BLOCK) k_aon(PathArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1296,6 +1656,7 @@ template <typename T, int BLOCK, bool SMEM>
 PathKernel sssp_kernel(int variant) {
   if (variant == kSsspRounds) return k_sssp<T, BLOCK, SMEM>;
   if (variant == kSsspAsync) return k_sssp_async<T, BLOCK, SMEM>;
+  if (variant == kSsspNearFarQueue) return k_sssp_nfq<T, BLOCK, SMEM>;
   return k_sssp_nf<T, BLOCK, SMEM>;
 }
 
@@ -1323,9 +1684,10 @@ cudaError_t launch_aon_t(const PathArgs& a, int grid, size_t smem, cudaStream_t 
 
 }  // namespace
 
-size_t sssp_smem_bytes(int n1, bool fp64) {
+size_t sssp_smem_bytes(int n1, bool fp64, int variant) {
   const size_t words = (static_cast<size_t>(n1) + 31) / 32;
-  return align16((fp64 ? 8 : 4) * static_cast<size_t>(n1)) + 2 * 4 * words;
+  const size_t ring = variant == kSsspNearFarQueue ? sizeof(unsigned short) * kQCap : 0;
+  return align16((fp64 ? 8 : 4) * static_cast<size_t>(n1)) + 2 * 4 * words + ring;
 }
 
 size_t aon_smem_bytes(int n1) {
@@ -1340,7 +1702,7 @@ int max_smem_optin(int device) {
 
 cudaError_t launch_sssp(const PathArgs& a, bool fp64, int grid, int block, bool smem,
                         int variant, cudaStream_t s) {
-  const size_t bytes = sssp_smem_bytes(a.g.n1, fp64);
+  const size_t bytes = sssp_smem_bytes(a.g.n1, fp64, variant);
 #define TAPGPU_SSSP_CASE(B)                                                              \
   if (block == B) {                                                                      \
     if (fp64) return smem ? launch_sssp_t<double, B, true>(a, grid, bytes, variant, s)   \
@@ -1394,7 +1756,7 @@ int occ_aon_t(size_t smem) {
 }
 
 int sssp_occupancy(bool fp64, int block, bool smem, int n1, int variant) {
-  const size_t bytes = sssp_smem_bytes(n1, fp64);
+  const size_t bytes = sssp_smem_bytes(n1, fp64, variant);
 #define TAPGPU_OCC(B)                                                                     \
   if (block == B) {                                                                       \
     if (fp64) return smem ? occ_sssp_t<double, B, true>(bytes, variant)                   \

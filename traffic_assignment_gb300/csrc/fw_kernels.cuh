@@ -139,7 +139,7 @@ struct LinkArgs {
 };
 
 // launch helpers (implemented in fw_kernels.cu)
-size_t sssp_smem_bytes(int n1, bool fp64);
+size_t sssp_smem_bytes(int n1, bool fp64, int variant = 0);
 size_t aon_smem_bytes(int n1);
 int max_smem_optin(int device);
 // shortest-path kernel variants
@@ -147,7 +147,9 @@ enum : int {
   kSsspRounds = 1,  // bulk-synchronous label-correction rounds (k_sssp)
   kSsspAsync = 2,   // warp-owned frontier words, no per-round barrier (k_sssp_async)
   kSsspNearFar = 3, // asynchronous near set below a rising threshold (k_sssp_nf)
+  kSsspNearFarQueue = 4,  // near-far with a FIFO ring of near nodes (k_sssp_nfq), <= 65535 nodes
 };
+constexpr int kQueueSlots = 1024;  // ring slots of k_sssp_nfq
 cudaError_t launch_sssp(const PathArgs& a, bool fp64, int grid, int block, bool smem,
                         int variant, cudaStream_t s);
 cudaError_t launch_aon(const PathArgs& a, bool fp64, int grid, int block, bool smem,

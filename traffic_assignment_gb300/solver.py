@@ -75,7 +75,8 @@ class Solver:
         opt.record_tape = 1 if record_tape else 0
         opt.tape_capacity = tape_capacity
         opt.global_scratch = 1 if global_scratch else 0
-        opt.sssp_variant = {"default": 0, "rounds": 1, "async": 2, "nearfar": 3}[sssp_variant]
+        opt.sssp_variant = {"default": 0, "rounds": 1, "async": 2, "nearfar": 3,
+                            "nearfar_queue": 4}[sssp_variant]
         opt.nf_delta = float(nf_delta)
         opt.line_search = {"reference": 0, "exact": 1}[line_search]
         opt.tape_checkpoint = int(tape_checkpoint)
@@ -230,13 +231,14 @@ class Solver:
         out = {f"{k}_ms": float(ms[i]) for i, k in enumerate(names)}
         out.update({f"{k}_launches": int(n[i]) for i, k in enumerate(names)})
         out["kernel_launches"] = int(kl[0])
-        st = np.zeros(5, np.int64)
+        st = np.zeros(6, np.int64)
         K.check(self.L.tapgpu_get_path_stats(self.h, K.ptr(st, K.I64P)))
         out["sssp_rounds"] = int(st[0])
         out["sssp_tasks"] = int(st[1])
         out["sssp_expansions"] = int(st[2])
         out["sssp_idle_polls"] = int(st[3])
         out["sssp_batches"] = int(st[4])
+        out["sssp_scanned"] = int(st[5])
         return out
 
     def profile_iteration(self, reps: int = 5) -> Dict[str, float]:
