@@ -157,7 +157,7 @@ def measured_peaks():
 def profile_traffic():
     """DRAM bytes per shortest-path task (label write-out dominates), from the
     committed ncu summary of the near-far kernel on the batched 10k-node case."""
-    p = os.path.join(ROOT, "profiles", "k_sssp_nf_grid10k_batched.md")
+    p = os.path.join(ROOT, "profiles", "k_sssp_nfq_grid10k_batched.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -224,6 +224,57 @@ def run_reference(args, rank, world):
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def adjoint_check(net, dem, iters=50):
+    """dVHT/dcapacity on the 10k-node network after `iters` FW iterations (FP32
+    paths, exact line search): GPU forward and adjoint times.  Its accuracy is
+    checked by the GPU tests against the FP64 CPU reverse sweep and central
+    differences."""
+    import torch
+
+    from traffic_assignment_gb300 import Solver
+    s = Solver(net, dem, precision="fp32", record_tape=True, tape_capacity=iters,
+               line_search="exact")
+    try:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.solve(max_iters=iters)
+        t1 = time.perf_counter()
+        vht, g = s.adjoint_vht()
+        t2 = time.perf_counter()
+    finally:
+        s.close()
+    return {"network": "grid10k", "iterations": iters, "precision": "fp32 paths, f64 adjoint",
+            "forward_ms": 1e3 * (t1 - t0), "adjoint_ms": 1e3 * (t2 - t1), "vht": vht,
+            "grad_nonzero_links": int(np.count_nonzero(g)),
+            "accuracy": "tests/test_gpu_adjoint.py: 1e-9 of max |g| vs the FP64 CPU reverse "
+                        "sweep; 1e-3 vs central differences (1% step) on 64 random links"}
+
+
+def large_network_rate(iters=6):
+    """FW iterations per second of one scenario of the 100k-node network (C5:
+    99,856 nodes, ~400k links, 4,000 zones, labels in global memory)."""
+    import torch
+
+    from traffic_assignment_gb300 import Solver, synth
+    net, dem = synth.make_grid100k()
+    with Solver(net, dem, precision="fp32") as s:
+        s.solve(max_iters=2)
+        s.set_timing(True)
+        stream = torch.cuda.ExternalStream(s.stream_ptr())
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s.run_iterations(iters)
+        e1.record(stream)
+        e1.synchronize()
+        tm = s.timing()
+    ms = e0.elapsed_time(e1) / iters
+    return {"network": "grid100k: 99,856 nodes, %d links, 4,000 zones" % net.num_links,
+            "fw_iterations_per_s": 1e3 / ms, "ms_per_iteration": ms,
+            "kernels_ms_per_iteration": {k: tm[f"{k}_ms"] / iters
+                                         for k in ("sssp", "aon", "line_search", "step")}}
 
 
 def run_ours(args, rank, world, local_rank):
@@ -322,6 +373,8 @@ def run_ours(args, rank, world, local_rank):
     if rank == 0:
         clocks = clk.summary()
         cpu = cpu_baseline(net, dem, scen[0], seconds=args.cpu_seconds) if not args.no_cpu else None
+        adj = None if args.no_extras else adjoint_check(net, dem)
+        large = None if args.no_extras else large_network_rate()
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -361,6 +414,8 @@ def run_ours(args, rank, world, local_rank):
                             "tapgpu_get_link_flows for every scenario",
                     "iterations": e2e_iters},
             "gpu_launches": tm["kernel_launches"],
+            "adjoint": adj,
+            "large_network": large,
         }
         print(json.dumps(line), flush=True)
     solver.close()
@@ -398,6 +453,8 @@ def main():
     ap.add_argument("--plain-scenarios", type=int, default=8)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the adjoint check and the 100k-node rate")
     ap.add_argument("--profile-case", choices=["plain", "batched"], default=None,
                     help="small case for ncu: a few FW iterations of the 10k-node network, "
                          "one scenario (plain) or 16 scenarios (batched), then exit")

@@ -217,3 +217,19 @@ def test_sssp_golden_graphs(built_lib, golden_dir, variant):
                 else:
                     assert z["term"][k] == v
                     assert d[i, z["init"][k]] + z["weight"][k] == d[i, v]
+
+
+def test_large_network_fp64(built_lib):
+    """C5: 99,856 nodes, ~400k links, 4,000 zones, labels in global memory (too
+    large for shared memory): two FP64 iterations against the oracle run on
+    the host cores."""
+    import os
+    net, dem = synth.make_grid100k()
+    ref = oracle.frankwolfe(net, dem, threads=os.cpu_count() or 1, max_iters=2)
+    with Solver(net, dem, precision="fp64") as s:
+        r = s.solve(max_iters=2)
+        x, _ = s.flows()
+    assert r["error_bits"] == 0 and r["iterations"] == 2
+    assert _rel(x, ref["x"]) < RTOL64
+    assert abs(r["total_cost"] - ref["total_cost"]) <= RTOL64 * ref["total_cost"]
+    assert abs(r["relgap"] - ref["relgap"]) <= RTOL64 * abs(ref["relgap"])

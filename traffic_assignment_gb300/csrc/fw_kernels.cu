@@ -159,6 +159,7 @@ __device__ __forceinline__ RevEdges<double> rev_edges_of<double>(const PathArgs&
 }
 
 constexpr int kEdgeGroup = 4;  // edge records fetched together before relaxing
+constexpr int kNoPred = 0x7fffffff;  // no tight in-link seen yet
 
 // Relax the out-links of v; returns 1 if any head label dropped.  The edge
 // records of a group are all requested before the first atomic so that
@@ -776,17 +777,22 @@ constexpr int kMaxSlotSpins = 1 << 20;       // bound on waiting for one slot
 // slot whose previous node has been claimed but not yet read).
 template <int BLOCK>
 __device__ __forceinline__ void ring_push(unsigned short* ring, unsigned* qhead, unsigned* qtail,
-                                          int v, int* err) {
+                                          int v, int* err, int* ovf) {
   if constexpr (BLOCK >= kQCap) {
-    return;  // no room for a margin of one slot per thread: the bitmap alone
+    *reinterpret_cast<volatile int*>(ovf) = 1;  // no room for a margin: the bitmap alone
+    return;
   } else {
-    if (vload(qtail) - vload(qhead) >= static_cast<unsigned>(kQCap - BLOCK)) return;
+    if (vload(qtail) - vload(qhead) >= static_cast<unsigned>(kQCap - BLOCK)) {
+      *reinterpret_cast<volatile int*>(ovf) = 1;  // v waits in the bitmap only
+      return;
+    }
     const unsigned pos = atomicAdd(qtail, 1u);
     volatile unsigned short* slot = ring + (pos & (kQCap - 1));
     int spins = 0;
     while (*slot != kQEmpty) {  // the previous lap's node is being read right now
-      if (++spins > kMaxSlotSpins) {
+      if (++spins > kMaxSlotSpins) {  // that node may lose its entry: scan the bitmap
         atomicOr(err, kErrRounds);
+        *reinterpret_cast<volatile int*>(ovf) = 1;
         break;
       }
     }
@@ -799,7 +805,8 @@ __device__ __forceinline__ int relax_range_nfq(int src, int e0, int e1, int firs
                                                const Edges<T>& ed, typename DT<T>::U* dist,
                                                unsigned* near, unsigned* far, T du,
                                                typename DT<T>::U thr_bits, unsigned short* ring,
-                                               unsigned* qhead, unsigned* qtail, int* err) {
+                                               unsigned* qhead, unsigned* qtail, int* err,
+                                               int* ovf) {
   using U = typename DT<T>::U;
   int pushes = 0;
   for (int b = e0; b < e1; b += kEdgeGroup) {
@@ -822,7 +829,7 @@ __device__ __forceinline__ int relax_range_nfq(int src, int e0, int e1, int firs
               const unsigned prev = atomicOr(near + (h >> 5), bit);
               if (!(prev & bit)) {
                 ++pushes;
-                ring_push<BLOCK>(ring, qhead, qtail, h, err);
+                ring_push<BLOCK>(ring, qhead, qtail, h, err, ovf);
               }
             }
           } else if (!(vload(far + (h >> 5)) & bit)) {
@@ -843,8 +850,8 @@ __device__ __forceinline__ void nfq_expand(const PathArgs& a, int src, int F, co
                                            typename DT<T>::U* dist, unsigned* near,
                                            unsigned* far, typename DT<T>::U thr,
                                            unsigned short* ring, unsigned* qhead,
-                                           unsigned* qtail, int* pending, int v, bool valid,
-                                           unsigned& expanded) {
+                                           unsigned* qtail, int* pending, int* ovf, int v,
+                                           bool valid, unsigned& expanded) {
   const int lane = threadIdx.x & 31;
   int e0 = 0, e1 = 0;
   if (valid && !(v < F && v != src)) {
@@ -863,7 +870,7 @@ __device__ __forceinline__ void nfq_expand(const PathArgs& a, int src, int F, co
   if (e1 > e0)
     pushes = relax_range_nfq<T, BLOCK>(src, e0, e1, F, ed, dist, near, far,
                                        DT<T>::val(vload(dist + v)), thr, ring, qhead, qtail,
-                                       a.err);
+                                       a.err, ovf);
   expanded += valid ? 1u : 0u;
   const int used = warp_sum(pushes);
   __syncwarp();
@@ -883,6 +890,7 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
   __shared__ int pending;
   __shared__ U sh_min;
   __shared__ unsigned qhead, qtail;
+  __shared__ int ovf;  // some near node of this phase is in the bitmap only
   const int n1 = a.g.n1;
   const int nwords = (n1 + 31) >> 5;
   unsigned char* base =
@@ -925,6 +933,7 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
       ring[0] = static_cast<unsigned short>(src);
       qhead = 0u;
       qtail = 1u;
+      ovf = 0;
     }
     __syncthreads();
     U thr = DT<T>::bits(delta);
@@ -965,16 +974,18 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
               v = q;
               const unsigned bit = 1u << (v & 31);
               valid = (atomicAnd(near + (v >> 5), ~bit) & bit) != 0u;
-            } else {
+            } else {  // the entry never arrived: its node is found by the scan
               atomicOr(a.err, kErrRounds);
+              *reinterpret_cast<volatile int*>(&ovf) = 1;
             }
           }
           ++batches;
           nfq_expand<T, BLOCK>(a, src, F, ed, dist, near, far, thr, ring, &qhead, &qtail,
-                               &pending, v, valid, expanded);
+                               &pending, &ovf, v, valid, expanded);
         }
         // -- nodes that found the ring full: scan this warp's bitmap words ------
-        for (int j0 = 0; j0 < my_words; j0 += 32) {
+        const int scan_words = vload(&ovf) ? my_words : 0;
+        for (int j0 = 0; j0 < scan_words; j0 += 32) {
           const int j = j0 + lane;
           const int wi = warp + j * kWarps;
           unsigned word = 0u;
@@ -1010,7 +1021,7 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
             ++batches;
             scanned += valid ? 1u : 0u;
             nfq_expand<T, BLOCK>(a, src, F, ed, dist, near, far, thr, ring, &qhead, &qtail,
-                                 &pending, v, valid, expanded);
+                                 &pending, &ovf, v, valid, expanded);
           }
         }
         if (!claimed_any) {
@@ -1028,7 +1039,10 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
       int left = 0;
       for (int i = threadIdx.x; i < nwords; i += BLOCK) left |= (near[i] != 0u);
       if (__syncthreads_or(left)) {  // a warp left early: recount and resume
-        if (threadIdx.x == 0) pending = 0;
+        if (threadIdx.x == 0) {
+          pending = 0;
+          ovf = 1;  // the bits left may have no ring entry
+        }
         __syncthreads();
         int c = 0;
         for (int i = threadIdx.x; i < nwords; i += BLOCK) c += __popc(near[i]);
@@ -1041,7 +1055,10 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
         }
         continue;
       }
-      if (threadIdx.x == 0) sh_min = DT<T>::kInf;
+      if (threadIdx.x == 0) {
+        sh_min = DT<T>::kInf;
+        ovf = 0;  // every near node of the finished phase has been expanded
+      }
       __syncthreads();
       U mn = DT<T>::kInf;
       for (int i = threadIdx.x; i < nwords; i += BLOCK) {
@@ -1084,7 +1101,7 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
           while (tt) {
             const int bpos = __ffs(tt) - 1;
             tt &= tt - 1;
-            ring_push<BLOCK>(ring, &qhead, &qtail, (i << 5) + bpos, a.err);
+            ring_push<BLOCK>(ring, &qhead, &qtail, (i << 5) + bpos, a.err, &ovf);
           }
         }
       }
@@ -1145,37 +1162,58 @@ __global__ void __launch_bounds__(BLOCK) k_aon(PathArgs a) {
     const RevEdges<T> rv = rev_edges_of<T>(a, scen);
     const T* din = static_cast<const T*>(a.dist) + static_cast<size_t>(task - a.task_begin) * n1;
 
-    for (int v = threadIdx.x; v < n1; v += BLOCK) dS[v] = din[v];
+    // labels in, several loads in flight per thread; predecessors cleared
+    {
+      int v = threadIdx.x;
+      for (; v + 3 * BLOCK < n1; v += 4 * BLOCK) {
+        const T x0 = din[v], x1 = din[v + BLOCK], x2 = din[v + 2 * BLOCK], x3 = din[v + 3 * BLOCK];
+        dS[v] = x0;
+        dS[v + BLOCK] = x1;
+        dS[v + 2 * BLOCK] = x2;
+        dS[v + 3 * BLOCK] = x3;
+      }
+      for (; v < n1; v += BLOCK) dS[v] = din[v];
+    }
+    for (int v = threadIdx.x; v < n1; v += BLOCK) pred[v] = kNoPred;
     __syncthreads();
 
-    // Predecessor = lowest-numbered tight in-link from a strictly closer tail.
-    int pend = 0;
-    for (int v = threadIdx.x; v < n1; v += BLOCK) {
-      int p = -1;
-      const T dv = dS[v];
-      if (v != src && DT<T>::bits(dv) != DT<T>::kInf) {
-        p = -2;
-        const int i0 = __ldg(a.g.in_ptr + v);
-        const int i1 = __ldg(a.g.in_ptr + v + 1);
-        for (int b = i0; b < i1 && p == -2; b += kEdgeGroup) {
-          int uu[kEdgeGroup];
-          T ww[kEdgeGroup];
+    // Predecessor = lowest-numbered tight in-link from a strictly closer tail:
+    // one sweep over the reverse-star slots (contiguous records, in link order
+    // within a node), keeping the smallest tight link of each head.
+    {
+      const int m = a.g.m;
+      for (int i0 = threadIdx.x; i0 < m; i0 += kEdgeGroup * BLOCK) {
+        int vv[kEdgeGroup], uu[kEdgeGroup];
+        T ww[kEdgeGroup];
 #pragma unroll
-          for (int j = 0; j < kEdgeGroup; ++j)
-            if (b + j < i1) rv.load(b + j, uu[j], ww[j]);
-#pragma unroll
-          for (int j = 0; j < kEdgeGroup; ++j) {
-            if (b + j >= i1) break;
-            const int u = uu[j];
-            if (u < F && u != src) continue;
-            const T du = dS[u];
-            if (du < dv && DT<T>::add(du, ww[j]) == dv) {
-              p = rv.link(b + j);
-              break;
-            }
+        for (int j = 0; j < kEdgeGroup; ++j) {
+          const int i = i0 + j * BLOCK;
+          vv[j] = -1;
+          uu[j] = 0;
+          if (i < m) {
+            vv[j] = __ldg(a.g.in_head + i);
+            rv.load(i, uu[j], ww[j]);
           }
         }
-        if (p == -2) pend = 1;
+#pragma unroll
+        for (int j = 0; j < kEdgeGroup; ++j) {
+          const int v = vv[j], u = uu[j];
+          if (v < 0 || v == src || (u < F && u != src)) continue;
+          const T dv = dS[v], du = dS[u];
+          if (du < dv && DT<T>::add(du, ww[j]) == dv)
+            atomicMin(pred + v, rv.link(i0 + j * BLOCK));
+        }
+      }
+    }
+    __syncthreads();
+    int pend = 0;
+    for (int v = threadIdx.x; v < n1; v += BLOCK) {
+      int p = pred[v];
+      if (v == src || DT<T>::bits(dS[v]) == DT<T>::kInf) {
+        p = -1;
+      } else if (p == kNoPred) {
+        p = -2;
+        pend = 1;
       }
       pred[v] = p;
     }
@@ -1247,6 +1285,7 @@ __global__ void __launch_bounds__(BLOCK) k_aon(PathArgs a) {
         a.err_info[1] = dest;
         continue;
       }
+      const unsigned q_lo = static_cast<unsigned>(q), q_hi = static_cast<unsigned>(q >> 32);
       int v = dest;
       int steps = 0;
       while (v != src) {
@@ -1254,7 +1293,11 @@ __global__ void __launch_bounds__(BLOCK) k_aon(PathArgs a) {
           atomicOr(a.err, kErrWalk);
           break;
         }
-        atomicAdd(reinterpret_cast<unsigned long long*>(thr + v), q);
+        // 64-bit total as two native 32-bit adds; a wrapped low word carries
+        unsigned* t32 = reinterpret_cast<unsigned*>(thr + v);
+        const unsigned old_lo = atomicAdd(t32, q_lo);
+        const unsigned carry = old_lo + q_lo < old_lo ? 1u : 0u;
+        if (q_hi | carry) atomicAdd(t32 + 1, q_hi + carry);
         v = parent[v];
       }
     }

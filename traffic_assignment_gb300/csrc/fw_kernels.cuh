@@ -37,6 +37,7 @@ struct Graph {
   const int* tail;
   const int* in_ptr;
   const int* in_link;
+  const int* in_head;  // head node of each reverse-star slot
 };
 
 struct LinkParams {

@@ -120,6 +120,7 @@ Graph Ctx::graph() const {
   g.tail = tail;
   g.in_ptr = in_ptr;
   g.in_link = in_link;
+  g.in_head = in_head;
   return g;
 }
 
@@ -608,6 +609,7 @@ static int create_impl(const tapgpu_network* net, const tapgpu_demand* dem,
   TG_TRY(c->alloc_n(&c->tail, M));
   TG_TRY(c->alloc_n(&c->in_ptr, n1 + 1));
   TG_TRY(c->alloc_n(&c->in_link, M));
+  TG_TRY(c->alloc_n(&c->in_head, M));
   TG_TRY(c->alloc_n(&c->rpos, M));
   TG_TRY(c->alloc_n(&c->fft, M));
   TG_TRY(c->alloc_n(&c->alpha, M));
@@ -618,6 +620,11 @@ static int create_impl(const tapgpu_network* net, const tapgpu_demand* dem,
   TG_CUDA(cudaMemcpy(c->tail, c->h_tail.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
   TG_CUDA(cudaMemcpy(c->in_ptr, ip_in.data(), sizeof(int) * (n1 + 1), cudaMemcpyHostToDevice));
   TG_CUDA(cudaMemcpy(c->in_link, inl.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
+  {
+    std::vector<int> ih(M);
+    for (int i = 0; i < M; ++i) ih[i] = c->h_head[inl[i]];
+    TG_CUDA(cudaMemcpy(c->in_head, ih.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
+  }
   TG_CUDA(cudaMemcpy(c->rpos, c->h_rpos.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
   TG_CUDA(cudaMemcpy(c->fft, c->h_fft.data(), sizeof(double) * M, cudaMemcpyHostToDevice));
   TG_CUDA(cudaMemcpy(c->alpha, c->h_alpha.data(), sizeof(double) * M, cudaMemcpyHostToDevice));

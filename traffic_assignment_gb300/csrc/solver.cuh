@@ -31,6 +31,7 @@ struct Ctx {
 
   // device topology and link parameters
   int *row_ptr = nullptr, *head = nullptr, *tail = nullptr, *in_ptr = nullptr, *in_link = nullptr;
+  int* in_head = nullptr;  // head node of each reverse-star slot
   double *fft = nullptr, *alpha = nullptr, *beta = nullptr;
   unsigned char* ipow = nullptr;
 
