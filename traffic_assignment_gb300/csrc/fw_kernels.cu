@@ -20,6 +20,8 @@
 //  k_step      x += lambda*d, BPR cost and derivative update and the
 //              shortest-path weights for the next iteration
 //              (tap/tap_frankwolfe_pthread.c:737-739, tap/tap_functions.c:55-65).
+#include <type_traits>
+
 #include "fw_kernels.cuh"
 
 #include "bpr.cuh"
@@ -846,20 +848,36 @@ __device__ __forceinline__ int relax_range_nfq(int src, int e0, int e1, int firs
 // k_sssp_async: `pending` is raised by the out-degree before relaxing, so it
 // cannot reach zero while this warp may still push.
 template <typename T, int BLOCK>
-__device__ __forceinline__ void nfq_expand(const PathArgs& a, int src, int F, const Edges<T>& ed,
+__device__ __forceinline__ void nfq_expand(const PathArgs& a, const uint2* e4s, int src, int F,
+                                           const Edges<T>& ed,
                                            typename DT<T>::U* dist, unsigned* near,
                                            unsigned* far, typename DT<T>::U thr,
                                            unsigned short* ring, unsigned* qhead,
                                            unsigned* qtail, int* pending, int* ovf, int v,
                                            bool valid, unsigned& expanded) {
   const int lane = threadIdx.x & 31;
-  int e0 = 0, e1 = 0;
-  if (valid && !(v < F && v != src)) {
-    e0 = __ldg(a.g.row_ptr + v);
-    e1 = __ldg(a.g.row_ptr + v + 1);
+  const bool expand = valid && !(v < F && v != src);
+  // FP32 paths read the padded layout: degree and the first four records in
+  // one round trip; FP64 paths read the CSR records
+  constexpr bool kPadded = std::is_same<T, float>::value;
+  int deg = 0, e0 = 0;
+  uint2 r4[4];
+  if (expand) {
+    if constexpr (kPadded) {
+      deg = __ldg(a.g.out_deg + v);
+      const uint4* p = reinterpret_cast<const uint4*>(e4s + static_cast<size_t>(v) * 4);
+      const uint4 q0 = __ldg(p), q1 = __ldg(p + 1);
+      r4[0] = make_uint2(q0.x, q0.y);
+      r4[1] = make_uint2(q0.z, q0.w);
+      r4[2] = make_uint2(q1.x, q1.y);
+      r4[3] = make_uint2(q1.z, q1.w);
+    } else {
+      e0 = __ldg(a.g.row_ptr + v);
+      deg = __ldg(a.g.row_ptr + v + 1) - e0;
+    }
   }
   // out-degrees and claimed nodes in one sum (degrees < 2^25 per warp)
-  const int packed = warp_sum(((e1 - e0) << 6) | (valid ? 1 : 0));
+  const int packed = warp_sum((deg << 6) | (valid ? 1 : 0));
   const int reserve = packed >> 6, items = packed & 63;
   if (lane == 0) {
     atomicAdd(pending, reserve);
@@ -867,10 +885,48 @@ __device__ __forceinline__ void nfq_expand(const PathArgs& a, int src, int F, co
   }
   __syncwarp();
   int pushes = 0;
-  if (e1 > e0)
-    pushes = relax_range_nfq<T, BLOCK>(src, e0, e1, F, ed, dist, near, far,
-                                       DT<T>::val(vload(dist + v)), thr, ring, qhead, qtail,
-                                       a.err, ovf);
+  if (deg > 0) {
+    const T du = DT<T>::val(vload(dist + v));
+    if constexpr (kPadded) {
+      using U = typename DT<T>::U;
+      // groups of four: the padded records first, then (degree > 4, rare on
+      // road networks) the node's further CSR records in the same registers
+      for (int base = 0;;) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          if (base + j >= deg) break;
+          const int h = static_cast<int>(r4[j].x);
+          const U nb = DT<T>::bits(DT<T>::add(du, __uint_as_float(r4[j].y)));
+          if (nb < vload(dist + h)) {
+            const U old = atomicMin(dist + h, nb);
+            if (nb < old && !(h < F && h != src)) {
+              const unsigned bit = 1u << (h & 31);
+              if (nb < thr) {
+                if (!(vload(near + (h >> 5)) & bit)) {
+                  const unsigned prev = atomicOr(near + (h >> 5), bit);
+                  if (!(prev & bit)) {
+                    ++pushes;
+                    ring_push<BLOCK>(ring, qhead, qtail, h, a.err, ovf);
+                  }
+                }
+              } else if (!(vload(far + (h >> 5)) & bit)) {
+                atomicOr(far + (h >> 5), bit);
+              }
+            }
+          }
+        }
+        base += 4;
+        if (base >= deg) break;
+        const int c0 = __ldg(a.g.row_ptr + v) + base;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (base + j < deg) r4[j] = __ldg(ed.e + c0 + j);
+      }
+    } else {
+      pushes = relax_range_nfq<T, BLOCK>(src, e0, e0 + deg, F, ed, dist, near, far, du, thr,
+                                         ring, qhead, qtail, a.err, ovf);
+    }
+  }
   expanded += valid ? 1u : 0u;
   const int used = warp_sum(pushes);
   __syncwarp();
@@ -918,6 +974,8 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
     if (a.state && a.state[scen].done) continue;
     const int src = a.sources[task - slot * a.num_sources];
     const Edges<T> ed = edges_of<T>(a, scen);
+    // this scenario's padded records (FP32 paths only)
+    const uint2* e4s = a.e4 ? a.e4 + static_cast<size_t>(scen) * n1 * 4 : nullptr;
     unsigned expanded = 0;
     unsigned long long polls = 0, batches = 0, scanned = 0;
     int phases = 0;
@@ -980,7 +1038,7 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
             }
           }
           ++batches;
-          nfq_expand<T, BLOCK>(a, src, F, ed, dist, near, far, thr, ring, &qhead, &qtail,
+          nfq_expand<T, BLOCK>(a, e4s, src, F, ed, dist, near, far, thr, ring, &qhead, &qtail,
                                &pending, &ovf, v, valid, expanded);
         }
         // -- nodes that found the ring full: scan this warp's bitmap words ------
@@ -1020,7 +1078,7 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
               v = ((warp + (j0 + owner) * kWarps) << 5) + nth_set_bit(ow, jj - (oincl - __popc(ow)));
             ++batches;
             scanned += valid ? 1u : 0u;
-            nfq_expand<T, BLOCK>(a, src, F, ed, dist, near, far, thr, ring, &qhead, &qtail,
+            nfq_expand<T, BLOCK>(a, e4s, src, F, ed, dist, near, far, thr, ring, &qhead, &qtail,
                                  &pending, &ovf, v, valid, expanded);
           }
         }
@@ -1371,12 +1429,18 @@ __device__ __forceinline__ bool last_block(unsigned* arrive) {
   return sh_ticket == gridDim.x - 1;
 }
 
-// shortest-path weight of link k of the scenario at offset i - k
-__device__ __forceinline__ void write_weights(const LinkArgs& a, size_t i, int k, double t) {
+// shortest-path weight of link k of scenario scen in every record layout
+__device__ __forceinline__ void write_weights(const LinkArgs& a, int scen, int k, double t) {
+  const size_t i = static_cast<size_t>(scen) * a.m + k;
   if (a.e32) {
     const unsigned bits = __float_as_uint(__double2float_rn(t));
-    a.e32[i] = make_uint2(static_cast<unsigned>(__ldg(a.head + k)), bits);
+    const uint2 rec = make_uint2(static_cast<unsigned>(__ldg(a.head + k)), bits);
+    a.e32[i] = rec;
     a.r32[i - k + __ldg(a.rpos + k)] = make_uint2(static_cast<unsigned>(__ldg(a.tail + k)), bits);
+    if (a.e4) {
+      const int p = __ldg(a.ell_pos + k);
+      if (p >= 0) a.e4[static_cast<size_t>(scen) * a.n1 * 4 + p] = rec;
+    }
   }
   if (a.w64) a.w64[i] = t;
 }
@@ -1402,7 +1466,7 @@ __global__ void __launch_bounds__(kLinkBlock) k_init_flows(LinkArgs a, int from_
     a.t[off + k] = t;
     if (a.dtdx)
       a.dtdx[off + k] = bpr_dq(a.lp.fft[k], a.lp.alpha[k], a.lp.beta[k], a.lp.ipow[k], cap[k], x);
-    write_weights(a, off + k, k, t);
+    write_weights(a, scen, k, t);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     ScenState& st = a.state[scen];
@@ -1428,7 +1492,7 @@ __global__ void __launch_bounds__(kLinkBlock) k_set_free_flow(LinkArgs a) {
   const size_t off = static_cast<size_t>(scen) * a.m;
   for (int k = blockIdx.x * kLinkBlock + threadIdx.x; k < a.m; k += gridDim.x * kLinkBlock) {
     a.y_fx[off + k] = 0ull;
-    write_weights(a, off + k, k, a.lp.fft[k]);
+    write_weights(a, scen, k, a.lp.fft[k]);
   }
 }
 
@@ -1531,11 +1595,25 @@ __global__ void __launch_bounds__(kLinkBlock) k_ls_pass(LinkArgs a) {
     } else {
       d = a.d[off + k];
     }
+    if (a.ls_ratio && ip != 255) {
+      // FP32-path mode, integer power: t(x + lam d) = fft + (fft alpha) (x/c + lam d/c)^beta
+      // with one division per link instead of one per candidate (FP64 mode keeps
+      // the reference's form, tap/tap_functions.c:55-65)
+      const double ic = 1.0 / c;
+      const double r0 = x * ic, rd = d * ic, A = fft * al;
 #pragma unroll
-    for (int j = 0; j < kLsPerPass; ++j) {
-      const double lam = ls_candidate(a.ls_mode, e0, blo, bhi, j);
-      const double q = __dadd_rn(x, __dmul_rn(lam, d));
-      acc[4 + j] = __dadd_rn(acc[4 + j], __dmul_rn(bpr(fft, al, be, ip, c, q), d));
+      for (int j = 0; j < kLsPerPass; ++j) {
+        const double lam = ls_candidate(a.ls_mode, e0, blo, bhi, j);
+        const double p = bprf::int_pow(r0 + lam * rd, ip);
+        acc[4 + j] += (fft + A * p) * d;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < kLsPerPass; ++j) {
+        const double lam = ls_candidate(a.ls_mode, e0, blo, bhi, j);
+        const double q = __dadd_rn(x, __dmul_rn(lam, d));
+        acc[4 + j] = __dadd_rn(acc[4 + j], __dmul_rn(bpr(fft, al, be, ip, c, q), d));
+      }
     }
   }
   block_sum<kNumSums, kLinkBlock>(acc, sh);
@@ -1636,7 +1714,7 @@ __global__ void __launch_bounds__(kLinkBlock) k_step(LinkArgs a) {
     const double t = bpr(fft, al, be, ip, c, x);
     a.t[off + k] = t;
     if (a.dtdx) a.dtdx[off + k] = bpr_dq(fft, al, be, ip, c, x);
-    write_weights(a, off + k, k, t);
+    write_weights(a, scen, k, t);
     acc[0] = __dadd_rn(acc[0], __dmul_rn(x, t));
   }
   block_sum<1, kLinkBlock>(acc, sh);
@@ -1745,6 +1823,8 @@ int max_smem_optin(int device) {
 
 cudaError_t launch_sssp(const PathArgs& a, bool fp64, int grid, int block, bool smem,
                         int variant, cudaStream_t s) {
+  // FP32 paths of the queue variant read the padded records
+  if (variant == kSsspNearFarQueue && !fp64 && !a.e4) return cudaErrorInvalidValue;
   const size_t bytes = sssp_smem_bytes(a.g.n1, fp64, variant);
 #define TAPGPU_SSSP_CASE(B)                                                              \
   if (block == B) {                                                                      \

@@ -38,6 +38,7 @@ struct Graph {
   const int* in_ptr;
   const int* in_link;
   const int* in_head;  // head node of each reverse-star slot
+  const int* out_deg;  // out-degree of each node
 };
 
 struct LinkParams {
@@ -80,6 +81,7 @@ struct Demand {
 struct PathArgs {
   Graph g;
   const uint2* e32;             // [S][m] {head, f32 weight bits} when fp32 paths
+  const uint2* e4;              // [S][n1][4] the first four records of each node, or nullptr
   const uint2* r32;             // [S][m] {tail, f32 weight bits} in reverse-star order
   const double* w64;            // [S][m] when fp64 paths
   const int* sources;           // source nodes
@@ -115,6 +117,9 @@ struct LinkArgs {
   double* d;                    // [S][m]
   unsigned long long* y_fx;     // [S][m]
   uint2* e32;                   // [S][m] packed fp32 edge records, or nullptr
+  uint2* e4;                    // [S][n1][4] first four records of each node, or nullptr
+  const int* ell_pos;           // [m] slot of link k in its tail's four (-1: beyond the fourth)
+  int n1;
   uint2* r32;                   // [S][m] packed fp32 reverse records (with e32)
   const int* head;              // [m] head node of each link (for e32)
   const int* tail;              // [m] tail node of each link (for r32)
@@ -137,6 +142,7 @@ struct LinkArgs {
   int hist_cap;
   int ckpt_every;               // flows kept every ckpt_every iterations
   int ls_mode;                  // kLsReference or kLsExact
+  int ls_ratio;                 // FP32-path mode: candidates from x/c + lambda d/c (one division)
 };
 
 // launch helpers (implemented in fw_kernels.cu)

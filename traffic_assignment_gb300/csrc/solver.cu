@@ -121,6 +121,7 @@ Graph Ctx::graph() const {
   g.in_ptr = in_ptr;
   g.in_link = in_link;
   g.in_head = in_head;
+  g.out_deg = out_deg;
   return g;
 }
 
@@ -167,6 +168,7 @@ PathArgs Ctx::path_args(int nscen_slots) const {
   a.scratch_stride = 0;
   a.stats = timing ? path_stats : nullptr;
   a.nf_delta = nf_delta;
+  a.e4 = (!fp64 && sssp_variant == kSsspNearFarQueue) ? e4 : nullptr;
   return a;
 }
 
@@ -184,6 +186,9 @@ LinkArgs Ctx::link_args(int nscen) const {
   a.y_fx = yfx;
   a.e32 = fp64 ? nullptr : e32;
   a.r32 = fp64 ? nullptr : r32;
+  a.e4 = fp64 ? nullptr : e4;
+  a.ell_pos = ell_pos;
+  a.n1 = n1;
   a.head = head;
   a.tail = tail;
   a.rpos = rpos;
@@ -204,18 +209,20 @@ LinkArgs Ctx::link_args(int nscen) const {
   a.hist_cap = hist_cap;
   a.ckpt_every = ckpt_every;
   a.ls_mode = ls_mode;
+  a.ls_ratio = fp64 ? 0 : 1;
   return a;
 }
 
 int Ctx::ensure_scenarios(int S) {
   if (S <= S_cap) return TAPGPU_OK;
   // release the old per-scenario arrays
-  void* olds[] = {cap, x, t, d, dtdx, yfx, e32, r32, w64, state, partials, arrive, trace, scen_list,
+  void* olds[] = {cap, x, t, d, dtdx, yfx, e32, r32, e4, w64, state, partials, arrive, trace, scen_list,
                   x_hist, d_hist, lam_hist};
   for (void* p : olds) free_owned(this, p);
   cap = x = t = d = dtdx = nullptr;
   yfx = nullptr;
   e32 = nullptr;
+  e4 = nullptr;
   r32 = nullptr;
   w64 = nullptr;
   state = nullptr;
@@ -236,6 +243,9 @@ int Ctx::ensure_scenarios(int S) {
   {
     TG_TRY(alloc_n(&e32, sm));
     TG_TRY(alloc_n(&r32, sm));
+    const size_t s4 = static_cast<size_t>(S) * n1 * 4;
+    TG_TRY(alloc_n(&e4, s4));
+    TG_CUDA(cudaMemset(e4, 0, sizeof(uint2) * s4));
   }
   if (opt.record_tape) TG_TRY(alloc_n(&dtdx, sm));
   TG_TRY(alloc_n(&state, static_cast<size_t>(S)));
@@ -308,6 +318,7 @@ int Ctx::enqueue_paths(int nscen, bool load, const uint2* e32p, const uint2* r32
   for (int64_t t0 = 0; t0 < tasks; t0 += dist_tasks) {
     const int64_t t1 = std::min(tasks, t0 + dist_tasks);
     PathArgs a = path_args(nscen);
+    if (a.e4) a.e4 = e32p == e32 ? e4 : (e32p == api_e32 ? api_e4 : nullptr);
     a.e32 = e32p;
     a.r32 = r32p;
     a.w64 = w64p;
@@ -610,6 +621,8 @@ static int create_impl(const tapgpu_network* net, const tapgpu_demand* dem,
   TG_TRY(c->alloc_n(&c->in_ptr, n1 + 1));
   TG_TRY(c->alloc_n(&c->in_link, M));
   TG_TRY(c->alloc_n(&c->in_head, M));
+  TG_TRY(c->alloc_n(&c->out_deg, n1));
+  TG_TRY(c->alloc_n(&c->ell_pos, M));
   TG_TRY(c->alloc_n(&c->rpos, M));
   TG_TRY(c->alloc_n(&c->fft, M));
   TG_TRY(c->alloc_n(&c->alpha, M));
@@ -624,6 +637,15 @@ static int create_impl(const tapgpu_network* net, const tapgpu_demand* dem,
     std::vector<int> ih(M);
     for (int i = 0; i < M; ++i) ih[i] = c->h_head[inl[i]];
     TG_CUDA(cudaMemcpy(c->in_head, ih.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
+    std::vector<int> deg(n1), pos(M);
+    for (int v = 0; v < n1; ++v) deg[v] = rp[v + 1] - rp[v];
+    for (int k = 0; k < M; ++k) {
+      const int v = c->h_tail[k], j = k - rp[v];
+      pos[k] = j < 4 ? v * 4 + j : -1;
+    }
+    c->h_ell_pos = pos;
+    TG_CUDA(cudaMemcpy(c->out_deg, deg.data(), sizeof(int) * n1, cudaMemcpyHostToDevice));
+    TG_CUDA(cudaMemcpy(c->ell_pos, pos.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
   }
   TG_CUDA(cudaMemcpy(c->rpos, c->h_rpos.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
   TG_CUDA(cudaMemcpy(c->fft, c->h_fft.data(), sizeof(double) * M, cudaMemcpyHostToDevice));
@@ -696,6 +718,7 @@ static int create_impl(const tapgpu_network* net, const tapgpu_demand* dem,
   c->dist_tasks = std::min<int64_t>(chunk, std::max<int64_t>(Z, 1) * 4096);
   TG_TRY(c->alloc(&c->dist, tb * c->dist_tasks));
   TG_TRY(c->alloc_n(&c->api_e32, M));
+  TG_TRY(c->alloc_n(&c->api_e4, static_cast<size_t>(n1) * 4));
   TG_TRY(c->alloc_n(&c->api_r32, M));
   TG_TRY(c->alloc_n(&c->api_w64, M));
   TG_TRY(c->alloc_n(&c->api_yfx, M));
@@ -1101,6 +1124,11 @@ static int to_device_weights(Ctx* c, const double* weights) {
   TG_CUDA(cudaMemcpyAsync(c->api_w64, w.data(), sizeof(double) * c->M, cudaMemcpyHostToDevice,
                           c->stream));
   TG_CUDA(cudaMemcpyAsync(c->api_e32, wf.data(), sizeof(uint2) * c->M, cudaMemcpyHostToDevice,
+                          c->stream));
+  std::vector<uint2> w4(static_cast<size_t>(c->n1) * 4, make_uint2(0u, 0u));
+  for (int k = 0; k < c->M; ++k)
+    if (c->h_ell_pos[k] >= 0) w4[c->h_ell_pos[k]] = wf[k];
+  TG_CUDA(cudaMemcpyAsync(c->api_e4, w4.data(), sizeof(uint2) * w4.size(), cudaMemcpyHostToDevice,
                           c->stream));
   TG_CUDA(cudaStreamSynchronize(c->stream));
   return TAPGPU_OK;

@@ -32,6 +32,9 @@ struct Ctx {
   // device topology and link parameters
   int *row_ptr = nullptr, *head = nullptr, *tail = nullptr, *in_ptr = nullptr, *in_link = nullptr;
   int* in_head = nullptr;  // head node of each reverse-star slot
+  int* out_deg = nullptr;  // out-degree of each node
+  int* ell_pos = nullptr;  // slot of each link among its tail's first four (-1: beyond)
+  std::vector<int> h_ell_pos;
   double *fft = nullptr, *alpha = nullptr, *beta = nullptr;
   unsigned char* ipow = nullptr;
 
@@ -56,6 +59,7 @@ struct Ctx {
   unsigned long long* yfx = nullptr;
   uint2* e32 = nullptr;  // packed {head, f32 weight} per scenario and link
   uint2* r32 = nullptr;  // packed {tail, f32 weight} per scenario, reverse-star order
+  uint2* e4 = nullptr;   // per scenario, the first four records of each node (padded)
   int* rpos = nullptr;   // reverse-star slot of each link
   std::vector<int> h_rpos;
   double* w64 = nullptr;
@@ -87,6 +91,7 @@ struct Ctx {
   unsigned long long* path_stats = nullptr;  // [8] rounds, tasks, expansions, idle polls, batches
   // buffers of the one-shot API (weights in both precisions, loaded volumes)
   uint2* api_e32 = nullptr;
+  uint2* api_e4 = nullptr;
   uint2* api_r32 = nullptr;
   double* api_w64 = nullptr;
   unsigned long long* api_yfx = nullptr;
