@@ -1808,11 +1808,13 @@ cudaError_t launch_aon_t(const PathArgs& a, int grid, size_t smem, cudaStream_t 
 size_t sssp_smem_bytes(int n1, bool fp64, int variant) {
   const size_t words = (static_cast<size_t>(n1) + 31) / 32;
   const size_t ring = variant == kSsspNearFarQueue ? sizeof(unsigned short) * kQCap : 0;
-  return align16((fp64 ? 8 : 4) * static_cast<size_t>(n1)) + 2 * 4 * words + ring;
+  return align16(align16((fp64 ? 8 : 4) * static_cast<size_t>(n1)) + 2 * 4 * words + ring);
 }
 
+// Both sizes are also the stride between CTAs' slices of the global-memory
+// scratch, so they are rounded to 16 bytes (8-byte totals and labels).
 size_t aon_smem_bytes(int n1) {
-  return align16(8 * static_cast<size_t>(n1)) + 2 * 4 * static_cast<size_t>(n1);
+  return align16(align16(8 * static_cast<size_t>(n1)) + 2 * 4 * static_cast<size_t>(n1));
 }
 
 int max_smem_optin(int device) {
