@@ -1191,8 +1191,28 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
   }
 }
 
-template <typename T, int BLOCK, bool SMEM>
-__global__ void __launch_bounds__(BLOCK) k_aon(PathArgs a) {
+constexpr unsigned short kNoParent16 = 0xffffu;  // node ids are below 65535 in the compact layout
+
+template <bool COMPACT>
+__device__ __forceinline__ int parent_of(const int* parent, const unsigned short* par16, int v) {
+  if constexpr (COMPACT) {
+    const unsigned short p = par16[v];
+    return p == kNoParent16 ? -1 : static_cast<int>(p);
+  } else {
+    return parent[v];
+  }
+}
+
+// COMPACT (FP32 labels, at most 65535 nodes): 8 bytes per node hold the
+// labels and the predecessor search, then the 64-bit node totals; parents
+// are 16-bit and the predecessor links move to the task's slot of the label
+// buffer (its labels are in shared memory by then).  10 bytes per node let
+// two CTAs share an SM up to ~11,500 nodes, so that one task's longest walks
+// overlap another task's work.  Otherwise 16 bytes per node: totals (labels
+// first), predecessor links, parents.
+template <typename T, int BLOCK, bool SMEM, bool COMPACT>
+__global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathArgs a) {
+  static_assert(!COMPACT || sizeof(T) == 4, "the compact layout holds 4-byte labels");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int sh_task;
   const int n1 = a.g.n1;
@@ -1201,8 +1221,10 @@ __global__ void __launch_bounds__(BLOCK) k_aon(PathArgs a) {
            : static_cast<unsigned char*>(a.scratch) + static_cast<size_t>(blockIdx.x) * a.scratch_stride;
   T* dS = reinterpret_cast<T*>(base);                         // labels, then ...
   long long* thr = reinterpret_cast<long long*>(base);        // ... node throughput
-  int* pred = reinterpret_cast<int*>(base + align16(sizeof(long long) * n1));
-  int* parent = pred + n1;
+  int* pred = COMPACT ? reinterpret_cast<int*>(base + 4 * static_cast<size_t>(n1))
+                      : reinterpret_cast<int*>(base + align16(sizeof(long long) * n1));
+  int* parent = pred + n1;  // (16-byte layout)
+  unsigned short* par16 = reinterpret_cast<unsigned short*>(base + align16(8 * static_cast<size_t>(n1)));
   const int F = a.g.first_thru;
 
   for (;;) {
@@ -1219,6 +1241,9 @@ __global__ void __launch_bounds__(BLOCK) k_aon(PathArgs a) {
     const Edges<T> ed = edges_of<T>(a, scen);
     const RevEdges<T> rv = rev_edges_of<T>(a, scen);
     const T* din = static_cast<const T*>(a.dist) + static_cast<size_t>(task - a.task_begin) * n1;
+    // COMPACT: the slot's labels are copied below; it then holds scratch and the links
+    int* gslot = reinterpret_cast<int*>(const_cast<T*>(din));
+    int* scr = COMPACT ? gslot : parent;
 
     // labels in, several loads in flight per thread; predecessors cleared
     {
@@ -1296,14 +1321,14 @@ __global__ void __launch_bounds__(BLOCK) k_aon(PathArgs a) {
             break;
           }
         }
-        parent[v] = c;
+        scr[v] = c;
       }
       __syncthreads();
       int progress = 0, still = 0;
       for (int v = threadIdx.x; v < n1; v += BLOCK) {
         if (pred[v] != -2) continue;
-        if (parent[v] >= 0) {
-          pred[v] = parent[v];
+        if (scr[v] >= 0) {
+          pred[v] = scr[v];
           progress = 1;
         } else {
           still = 1;
@@ -1317,9 +1342,15 @@ __global__ void __launch_bounds__(BLOCK) k_aon(PathArgs a) {
         break;
       }
     }
+    __syncthreads();  // (COMPACT: the scratch reads of the loop above precede the links' writes)
     for (int v = threadIdx.x; v < n1; v += BLOCK) {
       const int p = pred[v];
-      parent[v] = p >= 0 ? __ldg(a.g.tail + p) : -1;
+      if constexpr (COMPACT) {
+        par16[v] = p >= 0 ? static_cast<unsigned short>(__ldg(a.g.tail + p)) : kNoParent16;
+        gslot[v] = p >= 0 ? p : -1;
+      } else {
+        parent[v] = p >= 0 ? __ldg(a.g.tail + p) : -1;
+      }
     }
     if (a.pred_out) {
       int* po = a.pred_out + static_cast<size_t>(task - a.task_begin) * n1;
@@ -1337,7 +1368,7 @@ __global__ void __launch_bounds__(BLOCK) k_aon(PathArgs a) {
       const unsigned long long q =
           static_cast<unsigned long long>(__ldg(a.dem.od_q + scen * a.dem.q_stride + j));
       if (q == 0 && a.dem.q_stride) continue;  // a demand scenario removed this OD pair
-      if (dest < 0 || dest >= n1 || parent[dest] < 0) {
+      if (dest < 0 || dest >= n1 || parent_of<COMPACT>(parent, par16, dest) < 0) {
         atomicOr(a.err, kErrNoPath);
         a.err_info[0] = src;
         a.err_info[1] = dest;
@@ -1356,14 +1387,14 @@ __global__ void __launch_bounds__(BLOCK) k_aon(PathArgs a) {
         const unsigned old_lo = atomicAdd(t32, q_lo);
         const unsigned carry = old_lo + q_lo < old_lo ? 1u : 0u;
         if (q_hi | carry) atomicAdd(t32 + 1, q_hi + carry);
-        v = parent[v];
+        v = parent_of<COMPACT>(parent, par16, v);
       }
     }
     __syncthreads();
     unsigned long long* y = a.y_fx + static_cast<size_t>(scen) * a.g.m;
     for (int v = threadIdx.x; v < n1; v += BLOCK) {
       const long long q = thr[v];
-      if (q != 0) atomicAdd(y + pred[v], static_cast<unsigned long long>(q));
+      if (q != 0) atomicAdd(y + (COMPACT ? gslot[v] : pred[v]), static_cast<unsigned long long>(q));
     }
   }
 }
@@ -1792,9 +1823,9 @@ cudaError_t launch_sssp_t(const PathArgs& a, int grid, size_t smem, int variant,
   return cudaGetLastError();
 }
 
-template <typename T, int BLOCK, bool SMEM>
+template <typename T, int BLOCK, bool SMEM, bool COMPACT>
 cudaError_t launch_aon_t(const PathArgs& a, int grid, size_t smem, cudaStream_t s) {
-  auto fn = k_aon<T, BLOCK, SMEM>;
+  auto fn = k_aon<T, BLOCK, SMEM, COMPACT>;
   if (SMEM) {
     cudaError_t e = allow_max_smem(fn);
     if (e != cudaSuccess) return e;
@@ -1813,8 +1844,12 @@ size_t sssp_smem_bytes(int n1, bool fp64, int variant) {
 
 // Both sizes are also the stride between CTAs' slices of the global-memory
 // scratch, so they are rounded to 16 bytes (8-byte totals and labels).
-size_t aon_smem_bytes(int n1) {
-  return align16(align16(8 * static_cast<size_t>(n1)) + 2 * 4 * static_cast<size_t>(n1));
+bool aon_compact(int n1, bool fp64) { return !fp64 && n1 <= 0xffff; }
+
+size_t aon_smem_bytes(int n1, bool fp64) {
+  const size_t n = static_cast<size_t>(n1);
+  if (aon_compact(n1, fp64)) return align16(align16(8 * n) + align16(2 * n));
+  return align16(align16(8 * n) + 2 * 4 * n);
 }
 
 int max_smem_optin(int device) {
@@ -1845,13 +1880,16 @@ cudaError_t launch_sssp(const PathArgs& a, bool fp64, int grid, int block, bool 
 
 cudaError_t launch_aon(const PathArgs& a, bool fp64, int grid, int block, bool smem,
                        cudaStream_t s) {
-  const size_t bytes = aon_smem_bytes(a.g.n1);
+  const size_t bytes = aon_smem_bytes(a.g.n1, fp64);
+  const bool compact = aon_compact(a.g.n1, fp64);
 #define TAPGPU_AON_CASE(B)                                                               \
   if (block == B) {                                                                      \
-    if (fp64) return smem ? launch_aon_t<double, B, true>(a, grid, bytes, s)             \
-                          : launch_aon_t<double, B, false>(a, grid, bytes, s);           \
-    return smem ? launch_aon_t<float, B, true>(a, grid, bytes, s)                        \
-                : launch_aon_t<float, B, false>(a, grid, bytes, s);                      \
+    if (fp64) return smem ? launch_aon_t<double, B, true, false>(a, grid, bytes, s)      \
+                          : launch_aon_t<double, B, false, false>(a, grid, bytes, s);    \
+    if (compact) return smem ? launch_aon_t<float, B, true, true>(a, grid, bytes, s)     \
+                             : launch_aon_t<float, B, false, true>(a, grid, bytes, s);   \
+    return smem ? launch_aon_t<float, B, true, false>(a, grid, bytes, s)                 \
+                : launch_aon_t<float, B, false, false>(a, grid, bytes, s);               \
   }
   TAPGPU_AON_CASE(256)
   TAPGPU_AON_CASE(512)
@@ -1870,9 +1908,9 @@ int occ_sssp_t(size_t smem, int variant) {
   return n;
 }
 
-template <typename T, int BLOCK, bool SMEM>
+template <typename T, int BLOCK, bool SMEM, bool COMPACT>
 int occ_aon_t(size_t smem) {
-  auto fn = k_aon<T, BLOCK, SMEM>;
+  auto fn = k_aon<T, BLOCK, SMEM, COMPACT>;
   if (SMEM && allow_max_smem(fn) != cudaSuccess) return 0;
   int n = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, BLOCK, SMEM ? smem : 0) != cudaSuccess)
@@ -1898,11 +1936,16 @@ int sssp_occupancy(bool fp64, int block, bool smem, int n1, int variant) {
 }
 
 int aon_occupancy(bool fp64, int block, bool smem, int n1) {
-  const size_t bytes = aon_smem_bytes(n1);
+  const size_t bytes = aon_smem_bytes(n1, fp64);
+  const bool compact = aon_compact(n1, fp64);
 #define TAPGPU_OCC(B)                                                                     \
   if (block == B) {                                                                       \
-    if (fp64) return smem ? occ_aon_t<double, B, true>(bytes) : occ_aon_t<double, B, false>(bytes); \
-    return smem ? occ_aon_t<float, B, true>(bytes) : occ_aon_t<float, B, false>(bytes);     \
+    if (fp64) return smem ? occ_aon_t<double, B, true, false>(bytes)                      \
+                          : occ_aon_t<double, B, false, false>(bytes);                    \
+    if (compact) return smem ? occ_aon_t<float, B, true, true>(bytes)                     \
+                             : occ_aon_t<float, B, false, true>(bytes);                   \
+    return smem ? occ_aon_t<float, B, true, false>(bytes)                                 \
+                : occ_aon_t<float, B, false, false>(bytes);                               \
   }
   TAPGPU_OCC(256)
   TAPGPU_OCC(512)

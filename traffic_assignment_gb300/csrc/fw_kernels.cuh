@@ -147,7 +147,8 @@ struct LinkArgs {
 
 // launch helpers (implemented in fw_kernels.cu)
 size_t sssp_smem_bytes(int n1, bool fp64, int variant = 0);
-size_t aon_smem_bytes(int n1);
+size_t aon_smem_bytes(int n1, bool fp64);
+bool aon_compact(int n1, bool fp64);  // 10-byte-per-node loading layout
 int max_smem_optin(int device);
 // shortest-path kernel variants
 enum : int {

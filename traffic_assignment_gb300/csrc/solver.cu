@@ -292,7 +292,7 @@ int Ctx::plan_launches() {
   // leave room for the kernels' static shared memory (a few words)
   const size_t room = optin > 1024 ? static_cast<size_t>(optin - 1024) : 0;
   sssp_smem = sssp_smem_bytes(n1, fp64, sssp_variant) <= room && !opt.global_scratch;
-  aon_smem = aon_smem_bytes(n1) <= room && !opt.global_scratch;
+  aon_smem = aon_smem_bytes(n1, fp64) <= room && !opt.global_scratch;
   int so = sssp_occupancy(fp64, sssp_block, sssp_smem, n1, sssp_variant);
   int ao = aon_occupancy(fp64, aon_block, aon_smem, n1);
   if (so <= 0 || ao <= 0) {
@@ -303,7 +303,7 @@ int Ctx::plan_launches() {
   aon_grid = ao * num_sms;
   size_t scratch = 0;
   if (!sssp_smem) scratch = std::max(scratch, sssp_smem_bytes(n1, fp64, sssp_variant) * sssp_grid);
-  if (!aon_smem) scratch = std::max(scratch, aon_smem_bytes(n1) * aon_grid);
+  if (!aon_smem) scratch = std::max(scratch, aon_smem_bytes(n1, fp64) * aon_grid);
   if (scratch) {
     TG_TRY(alloc(&path_scratch, scratch));
     path_scratch_bytes = scratch;
@@ -341,7 +341,7 @@ int Ctx::enqueue_paths(int nscen, bool load, const uint2* e32p, const uint2* r32
                         stream));
     if (measuring) TG_TRY(mark(0, false));
     a.counter = counters + 1;
-    a.scratch_stride = static_cast<long long>(aon_smem_bytes(n1));
+    a.scratch_stride = static_cast<long long>(aon_smem_bytes(n1, fp64));
     if (measuring) TG_TRY(mark(1, true));
     TG_CUDA(launch_aon(a, fp64, std::min(aon_grid, ntask), aon_block, aon_smem, stream));
     if (measuring) TG_TRY(mark(1, false));
@@ -1202,9 +1202,20 @@ int tapgpu_sssp(tapgpu_ctx* ctx, const double* weights, const int64_t* srcs, int
       break;
     }
     a.counter = c->counters + 1;
-    a.scratch_stride = static_cast<long long>(tapgpu::aon_smem_bytes(n1));
-    if (tapgpu::launch_aon(a, true, std::min(c->aon_grid, ns), c->aon_block, c->aon_smem,
-                           c->stream) != cudaSuccess) {
+    // FP64 labels: the 16-byte-per-node loading layout, whatever the context's
+    const size_t abytes = tapgpu::aon_smem_bytes(n1, true);
+    const bool a_smem = abytes + 1024 <= static_cast<size_t>(optin) && !c->opt.global_scratch;
+    int agrid = std::max(1, std::min(tapgpu::aon_occupancy(true, c->aon_block, a_smem, n1) *
+                                         c->num_sms, ns));
+    if (!a_smem) {
+      agrid = std::min<int>(agrid, static_cast<int>(c->path_scratch_bytes / abytes));
+      if (agrid < 1) {
+        rc = TAPGPU_ERR_UNSUPPORTED;
+        break;
+      }
+    }
+    a.scratch_stride = static_cast<long long>(abytes);
+    if (tapgpu::launch_aon(a, true, agrid, c->aon_block, a_smem, c->stream) != cudaSuccess) {
       rc = TAPGPU_ERR_CUDA;
       break;
     }
@@ -1374,7 +1385,7 @@ int tapgpu_profile_iteration(tapgpu_ctx* ctx, int reps, float* ms) {
                         c->sssp_smem, c->sssp_variant, c->stream);
     cudaEventRecord(ev[1], c->stream);
     a.counter = c->counters + 1;
-    a.scratch_stride = static_cast<long long>(tapgpu::aon_smem_bytes(c->n1));
+    a.scratch_stride = static_cast<long long>(tapgpu::aon_smem_bytes(c->n1, c->fp64));
     tapgpu::launch_aon(a, c->fp64, std::min<int64_t>(c->aon_grid, tasks), c->aon_block,
                        c->aon_smem, c->stream);
     cudaEventRecord(ev[2], c->stream);
