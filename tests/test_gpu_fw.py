@@ -1,6 +1,6 @@
 """GPU parity of the Frank-Wolfe loop against the CPU oracle (port of the reference).
 
-Tolerances (from the spec contract):
+Tolerances:
   FP64 mode       link flows within 1e-6 relative, relative gap and VHT within 1e-6
   FP32-path mode  link flows within 1e-4 relative (of the largest flow)
   shortest paths  labels bit-exact in FP64 (integer and continuous weights)
