@@ -771,14 +771,18 @@ __global__ void __launch_bounds__(BLOCK) k_sssp_nf(PathArgs a) {
 // bitmap, where the word scan of k_sssp_nf still finds it.  The ring is an
 // accelerator only: losing an entry cannot lose a node.
 constexpr int kQCap = kQueueSlots;           // ring slots
-constexpr unsigned short kQEmpty = 0xffffu;  // a free slot (node ids are < 0xffff)
+// a free ring slot: all ones (16-bit entries serve networks below 65535 nodes)
+template <typename R>
+struct QEmpty {
+  static constexpr R value = static_cast<R>(~static_cast<R>(0));
+};
 constexpr int kMaxSlotSpins = 1 << 20;       // bound on waiting for one slot
 
 // Append v to the ring unless fewer than BLOCK slots are free (one per
 // thread that may be appending at the same time, so no append overruns a
 // slot whose previous node has been claimed but not yet read).
-template <int BLOCK>
-__device__ __forceinline__ void ring_push(unsigned short* ring, unsigned* qhead, unsigned* qtail,
+template <int BLOCK, typename R>
+__device__ __forceinline__ void ring_push(R* ring, unsigned* qhead, unsigned* qtail,
                                           int v, int* err, int* ovf) {
   if constexpr (BLOCK >= kQCap) {
     *reinterpret_cast<volatile int*>(ovf) = 1;  // no room for a margin: the bitmap alone
@@ -789,24 +793,24 @@ __device__ __forceinline__ void ring_push(unsigned short* ring, unsigned* qhead,
       return;
     }
     const unsigned pos = atomicAdd(qtail, 1u);
-    volatile unsigned short* slot = ring + (pos & (kQCap - 1));
+    volatile R* slot = ring + (pos & (kQCap - 1));
     int spins = 0;
-    while (*slot != kQEmpty) {  // the previous lap's node is being read right now
+    while (*slot != QEmpty<R>::value) {  // the previous lap's node is being read right now
       if (++spins > kMaxSlotSpins) {  // that node may lose its entry: scan the bitmap
         atomicOr(err, kErrRounds);
         *reinterpret_cast<volatile int*>(ovf) = 1;
         break;
       }
     }
-    *slot = static_cast<unsigned short>(v);
+    *slot = static_cast<R>(v);
   }
 }
 
-template <typename T, int BLOCK>
+template <typename T, int BLOCK, typename R>
 __device__ __forceinline__ int relax_range_nfq(int src, int e0, int e1, int first_thru,
                                                const Edges<T>& ed, typename DT<T>::U* dist,
                                                unsigned* near, unsigned* far, T du,
-                                               typename DT<T>::U thr_bits, unsigned short* ring,
+                                               typename DT<T>::U thr_bits, R* ring,
                                                unsigned* qhead, unsigned* qtail, int* err,
                                                int* ovf) {
   using U = typename DT<T>::U;
@@ -847,12 +851,12 @@ __device__ __forceinline__ int relax_range_nfq(int src, int e0, int e1, int firs
 // Expand each lane's claimed node (valid) with the reservation protocol of
 // k_sssp_async: `pending` is raised by the out-degree before relaxing, so it
 // cannot reach zero while this warp may still push.
-template <typename T, int BLOCK>
+template <typename T, int BLOCK, typename R>
 __device__ __forceinline__ void nfq_expand(const PathArgs& a, const uint2* e4s, int src, int F,
                                            const Edges<T>& ed,
                                            typename DT<T>::U* dist, unsigned* near,
                                            unsigned* far, typename DT<T>::U thr,
-                                           unsigned short* ring, unsigned* qhead,
+                                           R* ring, unsigned* qhead,
                                            unsigned* qtail, int* pending, int* ovf, int v,
                                            bool valid, unsigned& expanded) {
   const int lane = threadIdx.x & 31;
@@ -938,7 +942,7 @@ __device__ __forceinline__ void nfq_expand(const PathArgs& a, const uint2* e4s, 
 
 // five 256-thread CTAs per SM fit the shared memory of a 10k-node network:
 // keep registers to that occupancy
-template <typename T, int BLOCK, bool SMEM>
+template <typename T, int BLOCK, bool SMEM, typename R>
 __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) k_sssp_nfq(PathArgs a) {
   using U = typename DT<T>::U;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -955,7 +959,7 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
   U* dist = reinterpret_cast<U*>(base);
   unsigned* near = reinterpret_cast<unsigned*>(base + align16(sizeof(U) * n1));
   unsigned* far = near + nwords;
-  unsigned short* ring = reinterpret_cast<unsigned short*>(far + nwords);
+  R* ring = reinterpret_cast<R*>(far + nwords);
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   constexpr int kWarps = BLOCK / 32;
@@ -982,13 +986,13 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
 
     for (int v = threadIdx.x; v < n1; v += BLOCK) dist[v] = DT<T>::kInf;
     for (int i = threadIdx.x; i < 2 * nwords; i += BLOCK) near[i] = 0u;
-    for (int i = threadIdx.x; i < kQCap; i += BLOCK) ring[i] = kQEmpty;
+    for (int i = threadIdx.x; i < kQCap; i += BLOCK) ring[i] = QEmpty<R>::value;
     __syncthreads();
     if (threadIdx.x == 0) {
       dist[src] = DT<T>::bits(T(0));
       near[src >> 5] = 1u << (src & 31);
       pending = 1;
-      ring[0] = static_cast<unsigned short>(src);
+      ring[0] = static_cast<R>(src);
       qhead = 0u;
       qtail = 1u;
       ovf = 0;
@@ -1023,12 +1027,12 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
           int v = 0;
           bool valid = false;
           if (lane < n) {
-            volatile unsigned short* sl = ring + ((h + static_cast<unsigned>(lane)) & (kQCap - 1));
-            unsigned short q = *sl;
+            volatile R* sl = ring + ((h + static_cast<unsigned>(lane)) & (kQCap - 1));
+            R q = *sl;
             int spins = 0;
-            while (q == kQEmpty && ++spins <= kMaxSlotSpins) q = *sl;
-            if (q != kQEmpty) {
-              *sl = kQEmpty;
+            while (q == QEmpty<R>::value && ++spins <= kMaxSlotSpins) q = *sl;
+            if (q != QEmpty<R>::value) {
+              *sl = QEmpty<R>::value;
               v = q;
               const unsigned bit = 1u << (v & 31);
               valid = (atomicAnd(near + (v >> 5), ~bit) & bit) != 0u;
@@ -1808,7 +1812,8 @@ template <typename T, int BLOCK, bool SMEM>
 PathKernel sssp_kernel(int variant) {
   if (variant == kSsspRounds) return k_sssp<T, BLOCK, SMEM>;
   if (variant == kSsspAsync) return k_sssp_async<T, BLOCK, SMEM>;
-  if (variant == kSsspNearFarQueue) return k_sssp_nfq<T, BLOCK, SMEM>;
+  if (variant == kSsspNearFarQueue) return k_sssp_nfq<T, BLOCK, SMEM, unsigned short>;
+  if (variant == kSsspNearFarQueueWide) return k_sssp_nfq<T, BLOCK, SMEM, unsigned>;
   return k_sssp_nf<T, BLOCK, SMEM>;
 }
 
@@ -1838,7 +1843,9 @@ cudaError_t launch_aon_t(const PathArgs& a, int grid, size_t smem, cudaStream_t 
 
 size_t sssp_smem_bytes(int n1, bool fp64, int variant) {
   const size_t words = (static_cast<size_t>(n1) + 31) / 32;
-  const size_t ring = variant == kSsspNearFarQueue ? sizeof(unsigned short) * kQCap : 0;
+  const size_t ring = variant == kSsspNearFarQueue       ? sizeof(unsigned short) * kQCap
+                      : variant == kSsspNearFarQueueWide ? sizeof(unsigned) * kQCap
+                                                         : 0;
   return align16(align16((fp64 ? 8 : 4) * static_cast<size_t>(n1)) + 2 * 4 * words + ring);
 }
 
@@ -1861,7 +1868,8 @@ int max_smem_optin(int device) {
 cudaError_t launch_sssp(const PathArgs& a, bool fp64, int grid, int block, bool smem,
                         int variant, cudaStream_t s) {
   // FP32 paths of the queue variant read the padded records
-  if (variant == kSsspNearFarQueue && !fp64 && !a.e4) return cudaErrorInvalidValue;
+  if ((variant == kSsspNearFarQueue || variant == kSsspNearFarQueueWide) && !fp64 && !a.e4)
+    return cudaErrorInvalidValue;
   const size_t bytes = sssp_smem_bytes(a.g.n1, fp64, variant);
 #define TAPGPU_SSSP_CASE(B)                                                              \
   if (block == B) {                                                                      \

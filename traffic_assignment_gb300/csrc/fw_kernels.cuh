@@ -155,7 +155,8 @@ enum : int {
   kSsspRounds = 1,  // bulk-synchronous label-correction rounds (k_sssp)
   kSsspAsync = 2,   // warp-owned frontier words, no per-round barrier (k_sssp_async)
   kSsspNearFar = 3, // asynchronous near set below a rising threshold (k_sssp_nf)
-  kSsspNearFarQueue = 4,  // near-far with a FIFO ring of near nodes (k_sssp_nfq), <= 65535 nodes
+  kSsspNearFarQueue = 4,  // near-far with a FIFO ring of near nodes (k_sssp_nfq)
+  kSsspNearFarQueueWide = 5,  // the same with 32-bit ring entries (chosen above 65535 nodes)
 };
 constexpr int kQueueSlots = 1024;  // ring slots of k_sssp_nfq
 cudaError_t launch_sssp(const PathArgs& a, bool fp64, int grid, int block, bool smem,

@@ -168,7 +168,9 @@ PathArgs Ctx::path_args(int nscen_slots) const {
   a.scratch_stride = 0;
   a.stats = timing ? path_stats : nullptr;
   a.nf_delta = nf_delta;
-  a.e4 = (!fp64 && sssp_variant == kSsspNearFarQueue) ? e4 : nullptr;
+  a.e4 = (!fp64 && (sssp_variant == kSsspNearFarQueue || sssp_variant == kSsspNearFarQueueWide))
+             ? e4
+             : nullptr;
   return a;
 }
 
@@ -283,11 +285,14 @@ int Ctx::plan_launches() {
                      ? opt.sssp_variant
                      : kSsspNearFarQueue;
   // the ring of the queue variant holds 16-bit node ids
-  if (sssp_variant == kSsspNearFarQueue && n1 > 0xffff) sssp_variant = kSsspNearFar;
-  const bool nf = sssp_variant == kSsspNearFar || sssp_variant == kSsspNearFarQueue;
+  if (sssp_variant == kSsspNearFarQueue && n1 > 0xffff) sssp_variant = kSsspNearFarQueueWide;
+  const bool nf = sssp_variant == kSsspNearFar || sssp_variant == kSsspNearFarQueue ||
+                  sssp_variant == kSsspNearFarQueueWide;
   sssp_block = opt.sssp_block > 0 ? opt.sssp_block : (nf ? 256 : 512);
   // the ring keeps one free slot per thread
-  if (sssp_variant == kSsspNearFarQueue && sssp_block >= kQueueSlots) sssp_block = 256;
+  if ((sssp_variant == kSsspNearFarQueue || sssp_variant == kSsspNearFarQueueWide) &&
+      sssp_block >= kQueueSlots)
+    sssp_block = 256;
   aon_block = opt.aon_block > 0 ? opt.aon_block : 1024;
   // leave room for the kernels' static shared memory (a few words)
   const size_t room = optin > 1024 ? static_cast<size_t>(optin - 1024) : 0;
