@@ -2,9 +2,14 @@
 
 Tolerances:
   FP64 mode       link flows within 1e-6 relative, relative gap and VHT within 1e-6
-  FP32-path mode  link flows within 1e-4 relative (of the largest flow)
+  FP32-path mode  link flows within 1e-4 relative (of the largest flow); on
+                  the 100k-node network, where FP32 labels break near-ties
+                  differently, VHT/objective within 1e-4, L1 flows within 1e-3
+                  and every OD pair on a shortest path (see test_large_network)
   shortest paths  labels bit-exact in FP64 (integer and continuous weights)
 """
+
+import os
 
 import numpy as np
 import pytest
@@ -195,7 +200,6 @@ def test_sssp_golden_graphs(built_lib, golden_dir, variant):
     """The reference's own SSSP test graphs (rmat.txt.martin, okuyama example)
     and an integer grid: labels equal sssp_pape_lll's (stored golden values)."""
     import glob
-    import os
     from traffic_assignment_gb300.synth import Network
     for path in sorted(glob.glob(os.path.join(golden_dir, "sssp_*.npz"))):
         z = np.load(path)
@@ -219,17 +223,40 @@ def test_sssp_golden_graphs(built_lib, golden_dir, variant):
                     assert d[i, z["init"][k]] + z["weight"][k] == d[i, v]
 
 
-def test_large_network_fp64(built_lib):
-    """C5: 99,856 nodes, ~400k links, 4,000 zones, labels in global memory (too
-    large for shared memory): two FP64 iterations against the oracle run on
-    the host cores."""
-    import os
+@pytest.fixture(scope="module")
+def large_network_reference():
     net, dem = synth.make_grid100k()
-    ref = oracle.frankwolfe(net, dem, threads=os.cpu_count() or 1, max_iters=2)
-    with Solver(net, dem, precision="fp64") as s:
+    return net, dem, oracle.frankwolfe(net, dem, threads=os.cpu_count() or 1, max_iters=2)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_large_network(built_lib, large_network_reference, precision):
+    """C5: 99,856 nodes, ~400k links, 4,000 zones, labels in global memory (too
+    large for shared memory) and, by default, the queue kernel with 32-bit ring
+    entries: two iterations against the oracle run on the host cores.
+
+    FP64 is held to flows, VHT and relative gap within 1e-6.  FP32 labels on
+    a network this size break near-ties (two routes within FP32 rounding of one
+    another) differently from FP64, and each broken tie moves one OD pair's
+    whole demand to the other route, so single links can differ by a percent
+    of the largest flow.  The FP32 bounds are therefore the ones that do not
+    depend on tie-breaking: VHT and objective within 1e-4, the L1 difference of
+    the flows within 1e-3 of their L1 norm, and, loading the oracle's own link
+    costs, a total cost equal to the oracle's shortest-path total within 1e-6
+    (every OD pair is sent along a shortest path)."""
+    net, dem, ref = large_network_reference
+    with Solver(net, dem, precision=precision) as s:
         r = s.solve(max_iters=2)
         x, _ = s.flows()
+        y = s.aon(ref["t"]) if precision == "fp32" else None
     assert r["error_bits"] == 0 and r["iterations"] == 2
-    assert _rel(x, ref["x"]) < RTOL64
-    assert abs(r["total_cost"] - ref["total_cost"]) <= RTOL64 * ref["total_cost"]
-    assert abs(r["relgap"] - ref["relgap"]) <= RTOL64 * abs(ref["relgap"])
+    if precision == "fp64":
+        assert _rel(x, ref["x"]) < RTOL64
+        assert abs(r["total_cost"] - ref["total_cost"]) <= RTOL64 * ref["total_cost"]
+        assert abs(r["relgap"] - ref["relgap"]) <= RTOL64 * abs(ref["relgap"])
+        return
+    assert abs(r["total_cost"] - ref["total_cost"]) <= RTOL32 * ref["total_cost"]
+    assert abs(r["objective"] - ref["objective"]) <= RTOL32 * abs(ref["objective"])
+    assert np.abs(x - ref["x"]).sum() <= 1e-3 * np.abs(ref["x"]).sum()
+    y_ref = oracle.aon(net, dem, ref["t"], threads=os.cpu_count() or 1)
+    assert abs(ref["t"] @ y - ref["t"] @ y_ref) <= RTOL64 * (ref["t"] @ y_ref)
