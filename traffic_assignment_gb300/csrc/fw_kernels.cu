@@ -794,15 +794,21 @@ __device__ __forceinline__ void ring_push(R* ring, unsigned* qhead, unsigned* qt
     }
     const unsigned pos = atomicAdd(qtail, 1u);
     volatile R* slot = ring + (pos & (kQCap - 1));
-    int spins = 0;
-    while (*slot != QEmpty<R>::value) {  // the previous lap's node is being read right now
-      if (++spins > kMaxSlotSpins) {  // that node may lose its entry: scan the bitmap
+    // wait while the previous lap's node is being read; the store is made
+    // inside the loop, so that no lane holds its entry back while another
+    // lane of its warp is still waiting
+    for (int spins = 0;; ++spins) {
+      if (*slot == QEmpty<R>::value) {
+        *slot = static_cast<R>(v);
+        break;
+      }
+      if (spins >= kMaxSlotSpins) {  // that node may lose its entry: scan the bitmap
         atomicOr(err, kErrRounds);
         *reinterpret_cast<volatile int*>(ovf) = 1;
+        *slot = static_cast<R>(v);
         break;
       }
     }
-    *slot = static_cast<R>(v);
   }
 }
 
@@ -981,7 +987,7 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
     // this scenario's padded records (FP32 paths only)
     const uint2* e4s = a.e4 ? a.e4 + static_cast<size_t>(scen) * n1 * 4 : nullptr;
     unsigned expanded = 0;
-    unsigned long long polls = 0, batches = 0, scanned = 0;
+    unsigned polls = 0, batches = 0, scanned = 0;  // per task: 32 bits suffice
     int phases = 0;
 
     for (int v = threadIdx.x; v < n1; v += BLOCK) dist[v] = DT<T>::kInf;
@@ -1001,7 +1007,7 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
     U thr = DT<T>::bits(delta);
 
     for (;;) {  // phases
-      long long idle = 0;
+      int idle = 0;
       for (;;) {
         int claimed_any = 0;
         // -- batches of up to 32 nodes from the ring ---------------------------
@@ -1028,12 +1034,19 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
           bool valid = false;
           if (lane < n) {
             volatile R* sl = ring + ((h + static_cast<unsigned>(lane)) & (kQCap - 1));
-            R q = *sl;
-            int spins = 0;
-            while (q == QEmpty<R>::value && ++spins <= kMaxSlotSpins) q = *sl;
-            if (q != QEmpty<R>::value) {
-              *sl = QEmpty<R>::value;
-              v = q;
+            // wait for the entry and take it out in the same step (no lane
+            // keeps a slot full while another lane of its warp waits)
+            int e = -1;
+            for (int spins = 0; spins <= kMaxSlotSpins; ++spins) {
+              const R q = *sl;
+              if (q != QEmpty<R>::value) {
+                *sl = QEmpty<R>::value;
+                e = q;
+                break;
+              }
+            }
+            if (e >= 0) {
+              v = e;
               const unsigned bit = 1u << (v & 31);
               valid = (atomicAnd(near + (v >> 5), ~bit) & bit) != 0u;
             } else {  // the entry never arrived: its node is found by the scan
@@ -1046,7 +1059,8 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
                                &pending, &ovf, v, valid, expanded);
         }
         // -- nodes that found the ring full: scan this warp's bitmap words ------
-        const int scan_words = vload(&ovf) ? my_words : 0;
+        // decisions on shared flags are made on lane 0's reading, for the whole warp
+        const int scan_words = __shfl_sync(kFull, vload(&ovf), 0) ? my_words : 0;
         for (int j0 = 0; j0 < scan_words; j0 += 32) {
           const int j = j0 + lane;
           const int wi = warp + j * kWarps;
@@ -1087,7 +1101,7 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
           }
         }
         if (!claimed_any) {
-          if (vload(&pending) <= 0) break;
+          if (__shfl_sync(kFull, vload(&pending), 0) <= 0) break;
           ++polls;
           if (++idle > kMaxIdlePolls) {
             if (lane == 0) atomicOr(a.err, kErrRounds);
@@ -1183,9 +1197,9 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
       for (int o = 16; o >= 1; o >>= 1) expanded += __shfl_down_sync(kFull, expanded, o);
       if (lane == 0) {
         atomicAdd(a.stats + 2, static_cast<unsigned long long>(expanded));
-        atomicAdd(a.stats + 3, polls);
-        atomicAdd(a.stats + 4, batches);
-        atomicAdd(a.stats + 5, scanned);
+        atomicAdd(a.stats + 3, static_cast<unsigned long long>(polls));
+        atomicAdd(a.stats + 4, static_cast<unsigned long long>(batches));
+        atomicAdd(a.stats + 5, static_cast<unsigned long long>(scanned));
       }
       if (threadIdx.x == 0) {
         atomicAdd(a.stats + 0, static_cast<unsigned long long>(phases));
