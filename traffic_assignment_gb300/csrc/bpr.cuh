@@ -21,6 +21,21 @@ __device__ __forceinline__ double int_pow(double r, int n) {
   return acc;
 }
 
+// r^n for the FP32-path forms, where rounding need not follow the reference:
+// the usual beta = 4 as two squarings
+__device__ __forceinline__ double int_pow_fast(double r, int n) {
+  if (n == 4) {
+    const double r2 = r * r;
+    return r2 * r2;
+  }
+  return int_pow(r, n);
+}
+
+// 1 / n, the integral's 1 / (beta + 1) for integer beta (beta = 4 without a division)
+__device__ __forceinline__ double inv_int(int n) {
+  return n == 5 ? 0.2 : 1.0 / static_cast<double>(n);
+}
+
 // r^beta; ip is beta when beta is an integer 0..15, else 255
 __device__ __forceinline__ double pow_p(double r, double beta, unsigned char ip) {
   return ip != 255 ? int_pow(r, ip) : pow(r, beta);

@@ -1630,6 +1630,12 @@ __global__ void __launch_bounds__(kLinkBlock) k_ls_pass(LinkArgs a) {
     const double x = a.x[off + k];
     const double fft = a.lp.fft[k], al = a.lp.alpha[k], be = a.lp.beta[k], c = cap[k];
     const unsigned char ip = a.lp.ipow[k];
+    // FP32-path mode, integer power: t(x + lam d) = fft + (fft alpha) (x/c + lam d/c)^beta
+    // with one division per link (FP64 mode keeps the reference's forms,
+    // tap/tap_functions.c:55-65, 112-126)
+    const bool ratio = a.ls_ratio && ip != 255;
+    const double ic = ratio ? 1.0 / c : 0.0;
+    const double A = fft * al;
     double d;
     if (a.pass == 0) {
       const double y = static_cast<double>(static_cast<long long>(a.y_fx[off + k])) * a.inv_scale;
@@ -1639,22 +1645,24 @@ __global__ void __launch_bounds__(kLinkBlock) k_ls_pass(LinkArgs a) {
       const double t = a.t[off + k];
       acc[0] = __dadd_rn(acc[0], __dmul_rn(t, d));
       acc[1] = __dadd_rn(acc[1], __dmul_rn(x, t));
-      acc[2] = __dadd_rn(acc[2], integral(fft, al, be, ip, c, x));
-      acc[3] = __dadd_rn(acc[3], __dmul_rn(bpr(fft, al, be, ip, c, __dadd_rn(x, d)), d));
+      if (ratio) {
+        // x fft (1 + alpha / (beta + 1) (x/c)^beta) and t(x + d) d
+        const double r0 = x * ic;
+        acc[2] += x * (fft + A * bprf::int_pow_fast(r0, ip) * bprf::inv_int(ip + 1));
+        acc[3] += (fft + A * bprf::int_pow_fast(r0 + d * ic, ip)) * d;
+      } else {
+        acc[2] = __dadd_rn(acc[2], integral(fft, al, be, ip, c, x));
+        acc[3] = __dadd_rn(acc[3], __dmul_rn(bpr(fft, al, be, ip, c, __dadd_rn(x, d)), d));
+      }
     } else {
       d = a.d[off + k];
     }
-    if (a.ls_ratio && ip != 255) {
-      // FP32-path mode, integer power: t(x + lam d) = fft + (fft alpha) (x/c + lam d/c)^beta
-      // with one division per link instead of one per candidate (FP64 mode keeps
-      // the reference's form, tap/tap_functions.c:55-65)
-      const double ic = 1.0 / c;
-      const double r0 = x * ic, rd = d * ic, A = fft * al;
+    if (ratio) {
+      const double r0 = x * ic, rd = d * ic;
 #pragma unroll
       for (int j = 0; j < kLsPerPass; ++j) {
         const double lam = ls_candidate(a.ls_mode, e0, blo, bhi, j);
-        const double p = bprf::int_pow(r0 + lam * rd, ip);
-        acc[4 + j] += (fft + A * p) * d;
+        acc[4 + j] += (fft + A * bprf::int_pow_fast(r0 + lam * rd, ip)) * d;
       }
     } else {
 #pragma unroll

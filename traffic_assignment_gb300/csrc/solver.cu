@@ -374,7 +374,7 @@ int Ctx::enqueue_iteration(int nscen) {
   const int passes = ls_mode == kLsExact ? kLsExactPasses : kLsPasses;
   for (int p = 0; p < passes; ++p) {
     la.pass = p;
-    TG_CUDA(launch_ls_pass(la, link_grid, stream));
+    TG_CUDA(launch_ls_pass(la, ls_grid(nscen), stream));
   }
   TG_CUDA(launch_ls_fallback(la, stream));
   TG_TRY(mark(2, false));
@@ -1397,7 +1397,7 @@ int tapgpu_profile_iteration(tapgpu_ctx* ctx, int reps, float* ms) {
     tapgpu::LinkArgs la = c->link_args(1);
     for (int p = 0; p < tapgpu::kLsPasses; ++p) {
       la.pass = p;
-      tapgpu::launch_ls_pass(la, c->link_grid, c->stream);
+      tapgpu::launch_ls_pass(la, c->ls_grid(1), c->stream);
     }
     tapgpu::launch_ls_fallback(la, c->stream);
     cudaEventRecord(ev[3], c->stream);

@@ -130,6 +130,13 @@ struct Ctx {
   double api_nf_delta = 1.0;  // the same for the weights of the one-shot API
   bool sssp_smem = true, aon_smem = true;
   int sssp_grid = 0, aon_grid = 0;
+  // line-search blocks per scenario: about 16 blocks per SM over the whole
+  // batch, so that a batch's threads each sum many links and the 16-value
+  // block reductions stay a small part of the FP64 work
+  int ls_grid(int nscen) const {
+    const int want = (16 * num_sms + nscen - 1) / (nscen > 0 ? nscen : 1);
+    return want < 1 ? 1 : (want > link_grid ? link_grid : want);
+  }
 
   std::vector<DevMem> owned;
 
