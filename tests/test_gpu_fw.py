@@ -134,14 +134,23 @@ def test_sssp_integer_weights_bit_exact(built_lib):
     np.testing.assert_array_equal(d, dref)
 
 
-def test_first_thru_node_respected(built_lib):
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_first_thru_node_respected(built_lib, precision):
+    """Zone-only nodes (below first_thru_node) carry no through paths, in
+    both precisions."""
     net, dem = synth.make_grid416_centroids()
+    assert net.first_thru_node > 1
     ref = oracle.frankwolfe(net, dem, threads=1, max_iters=25)
-    with Solver(net, dem, precision="fp64") as s:
+    with Solver(net, dem, precision=precision) as s:
         r = s.solve(max_iters=25)
         x, _ = s.flows()
-    assert _rel(x, ref["x"]) < RTOL64
-    assert abs(r["relgap"] - ref["relgap"]) <= RTOL64 * abs(ref["relgap"])
+    assert r["error_bits"] == 0
+    if precision == "fp64":
+        assert _rel(x, ref["x"]) < RTOL64
+        assert abs(r["relgap"] - ref["relgap"]) <= RTOL64 * abs(ref["relgap"])
+    else:
+        assert _rel(x, ref["x"]) < RTOL32
+        assert abs(r["total_cost"] - ref["total_cost"]) <= RTOL32 * abs(ref["total_cost"])
 
 
 def test_warm_start(built_lib, grid416):
