@@ -161,7 +161,10 @@ __device__ __forceinline__ RevEdges<double> rev_edges_of<double>(const PathArgs&
 }
 
 constexpr int kEdgeGroup = 4;  // edge records fetched together before relaxing
-constexpr int kNoPred = 0x7fffffff;  // no tight in-link seen yet
+// predecessor words of k_aon (real ones are below kPredRoot)
+constexpr unsigned kPredNone = 0xffffffffu;     // no tight in-link seen yet
+constexpr unsigned kPredPending = 0xfffffffeu;  // reached only over zero / absorbed costs
+constexpr unsigned kPredRoot = 0xfffffffdu;     // the source, or unreachable
 
 // Relax the out-links of v; returns 1 if any head label dropped.  The edge
 // records of a group are all requested before the first atomic so that
@@ -1275,7 +1278,12 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
       }
       for (; v < n1; v += BLOCK) dS[v] = din[v];
     }
-    for (int v = threadIdx.x; v < n1; v += BLOCK) pred[v] = kNoPred;
+    // Predecessor words: the link id, or (link << 16 | tail) when links and
+    // nodes both fit 16 bits (the compact layout), so that the parents need
+    // no lookup of the link's tail; the minimum still orders by link.
+    const bool pack = COMPACT && a.g.m <= 0xffff;
+    unsigned* up = reinterpret_cast<unsigned*>(pred);
+    for (int v = threadIdx.x; v < n1; v += BLOCK) up[v] = kPredNone;
     __syncthreads();
 
     // Predecessor = lowest-numbered tight in-link from a strictly closer tail:
@@ -1301,22 +1309,24 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
           const int v = vv[j], u = uu[j];
           if (v < 0 || v == src || (u < F && u != src)) continue;
           const T dv = dS[v], du = dS[u];
-          if (du < dv && DT<T>::add(du, ww[j]) == dv)
-            atomicMin(pred + v, rv.link(i0 + j * BLOCK));
+          if (du < dv && DT<T>::add(du, ww[j]) == dv) {
+            const unsigned k = static_cast<unsigned>(rv.link(i0 + j * BLOCK));
+            atomicMin(up + v, pack ? (k << 16) | static_cast<unsigned>(u) : k);
+          }
         }
       }
     }
     __syncthreads();
     int pend = 0;
     for (int v = threadIdx.x; v < n1; v += BLOCK) {
-      int p = pred[v];
+      unsigned p = up[v];
       if (v == src || DT<T>::bits(dS[v]) == DT<T>::kInf) {
-        p = -1;
-      } else if (p == kNoPred) {
-        p = -2;
+        p = kPredRoot;
+      } else if (p == kPredNone) {
+        p = kPredPending;
         pend = 1;
       }
-      pred[v] = p;
+      up[v] = p;
     }
     pend = __syncthreads_or(pend);
     // Rare: labels reached only over links too short to change them (zero or
@@ -1325,28 +1335,30 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
     int guard = 0;
     while (pend) {
       for (int v = threadIdx.x; v < n1; v += BLOCK) {
-        if (pred[v] != -2) continue;
-        int c = -2;
+        if (up[v] != kPredPending) continue;
+        unsigned c = kPredPending;
         const T dv = dS[v];
         const int i1 = __ldg(a.g.in_ptr + v + 1);
         for (int i = __ldg(a.g.in_ptr + v); i < i1; ++i) {
           const int k = __ldg(a.g.in_link + i);
           const int u = __ldg(a.g.tail + k);
           if (u < F && u != src) continue;
-          if (!(u == src || pred[u] >= 0)) continue;
+          if (!(u == src || up[u] < kPredRoot)) continue;
           if (DT<T>::add(dS[u], ed.weight(k)) == dv) {
-            c = k;
+            c = pack ? (static_cast<unsigned>(k) << 16) | static_cast<unsigned>(u)
+                     : static_cast<unsigned>(k);
             break;
           }
         }
-        scr[v] = c;
+        scr[v] = static_cast<int>(c);
       }
       __syncthreads();
       int progress = 0, still = 0;
       for (int v = threadIdx.x; v < n1; v += BLOCK) {
-        if (pred[v] != -2) continue;
-        if (scr[v] >= 0) {
-          pred[v] = scr[v];
+        if (up[v] != kPredPending) continue;
+        const unsigned c = static_cast<unsigned>(scr[v]);
+        if (c != kPredPending) {
+          up[v] = c;
           progress = 1;
         } else {
           still = 1;
@@ -1362,17 +1374,22 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
     }
     __syncthreads();  // (COMPACT: the scratch reads of the loop above precede the links' writes)
     for (int v = threadIdx.x; v < n1; v += BLOCK) {
-      const int p = pred[v];
+      const unsigned p = up[v];
+      const bool ok = p < kPredRoot;
       if constexpr (COMPACT) {
-        par16[v] = p >= 0 ? static_cast<unsigned short>(__ldg(a.g.tail + p)) : kNoParent16;
-        gslot[v] = p >= 0 ? p : -1;
+        par16[v] = ok ? static_cast<unsigned short>(pack ? (p & 0xffffu) : __ldg(a.g.tail + p))
+                      : kNoParent16;
+        gslot[v] = ok ? static_cast<int>(pack ? p >> 16 : p) : -1;
       } else {
-        parent[v] = p >= 0 ? __ldg(a.g.tail + p) : -1;
+        parent[v] = ok ? __ldg(a.g.tail + p) : -1;
       }
     }
     if (a.pred_out) {
       int* po = a.pred_out + static_cast<size_t>(task - a.task_begin) * n1;
-      for (int v = threadIdx.x; v < n1; v += BLOCK) po[v] = pred[v] >= 0 ? pred[v] : -1;
+      for (int v = threadIdx.x; v < n1; v += BLOCK) {
+        const unsigned p = up[v];
+        po[v] = p < kPredRoot ? static_cast<int>(pack ? p >> 16 : p) : -1;
+      }
     }
     __syncthreads();  // labels no longer needed: their space becomes the node totals
     if (!a.do_load) continue;
