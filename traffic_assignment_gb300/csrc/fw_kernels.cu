@@ -1236,6 +1236,7 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
   static_assert(!COMPACT || sizeof(T) == 4, "the compact layout holds 4-byte labels");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int sh_task;
+  __shared__ unsigned long long sh_red[BLOCK / 32];
   const int n1 = a.g.n1;
   unsigned char* base =
       SMEM ? smem_raw
@@ -1393,15 +1394,41 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
     }
     __syncthreads();  // labels no longer needed: their space becomes the node totals
     if (!a.do_load) continue;
-    for (int v = threadIdx.x; v < n1; v += BLOCK) thr[v] = 0;
-    __syncthreads();
+    const int j0 = __ldg(a.dem.od_ptr + sidx), j1 = __ldg(a.dem.od_ptr + sidx + 1);
+    const long long* oq = a.dem.od_q + scen * a.dem.q_stride;
+    // COMPACT (FP32 paths): 32-bit node totals in units of 2^kshift of the
+    // fixed point, kshift the smallest that keeps this origin's whole demand
+    // below 2^31, so that a walk step is one 32-bit add without a return
+    // value.  Each OD demand is rounded to the nearest unit (for a 10k-node
+    // network about 1e-6 trips; no bias, and the roundings of at most 2^31
+    // OD pairs keep every total below 2^32): far inside the FP32-path
+    // tolerance, and the sums stay exact integers, independent of order.
+    // Otherwise 64-bit totals.
+    unsigned* tot32 = reinterpret_cast<unsigned*>(base);
+    int kshift = 0;
+    if constexpr (COMPACT) {
+      unsigned long long tq = 0;
+      for (int j = j0 + threadIdx.x; j < j1; j += BLOCK)
+        tq += static_cast<unsigned long long>(__ldg(oq + j));
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) tq += __shfl_xor_sync(kFull, tq, o);
+      if ((threadIdx.x & 31) == 0) sh_red[threadIdx.x >> 5] = tq;
+      for (int v = threadIdx.x; v < n1; v += BLOCK) tot32[v] = 0u;
+      __syncthreads();
+      unsigned long long total = 0;
+#pragma unroll
+      for (int w = 0; w < BLOCK / 32; ++w) total += sh_red[w];
+      kshift = total ? 64 - __clzll(static_cast<long long>(total)) - 31 : 0;
+      if (kshift < 0) kshift = 0;
+    } else {
+      for (int v = threadIdx.x; v < n1; v += BLOCK) thr[v] = 0;
+      __syncthreads();
+    }
 
-    const int j1 = __ldg(a.dem.od_ptr + sidx + 1);
-    for (int j = __ldg(a.dem.od_ptr + sidx) + threadIdx.x; j < j1; j += BLOCK) {
+    for (int j = j0 + threadIdx.x; j < j1; j += BLOCK) {
       const int dest = __ldg(a.dem.od_dest + j);
       if (dest == src || !(__ldg(a.dem.od_dem + j) > 0.0)) continue;
-      const unsigned long long q =
-          static_cast<unsigned long long>(__ldg(a.dem.od_q + scen * a.dem.q_stride + j));
+      const unsigned long long q = static_cast<unsigned long long>(__ldg(oq + j));
       if (q == 0 && a.dem.q_stride) continue;  // a demand scenario removed this OD pair
       if (dest < 0 || dest >= n1 || parent_of<COMPACT>(parent, par16, dest) < 0) {
         atomicOr(a.err, kErrNoPath);
@@ -1409,27 +1436,48 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
         a.err_info[1] = dest;
         continue;
       }
-      const unsigned q_lo = static_cast<unsigned>(q), q_hi = static_cast<unsigned>(q >> 32);
-      int v = dest;
-      int steps = 0;
-      while (v != src) {
-        if (v < 0 || ++steps > n1) {
-          atomicOr(a.err, kErrWalk);
-          break;
+      if constexpr (COMPACT) {
+        const unsigned qk =
+            static_cast<unsigned>(kshift ? (q + (1ull << (kshift - 1))) >> kshift : q);
+        if (qk == 0) continue;  // below this task's unit
+        int v = dest;
+        int steps = 0;
+        while (v != src) {
+          if (v < 0 || ++steps > n1) {
+            atomicOr(a.err, kErrWalk);
+            break;
+          }
+          atomicAdd(tot32 + v, qk);
+          v = parent_of<COMPACT>(parent, par16, v);
         }
-        // 64-bit total as two native 32-bit adds; a wrapped low word carries
-        unsigned* t32 = reinterpret_cast<unsigned*>(thr + v);
-        const unsigned old_lo = atomicAdd(t32, q_lo);
-        const unsigned carry = old_lo + q_lo < old_lo ? 1u : 0u;
-        if (q_hi | carry) atomicAdd(t32 + 1, q_hi + carry);
-        v = parent_of<COMPACT>(parent, par16, v);
+      } else {
+        const unsigned q_lo = static_cast<unsigned>(q), q_hi = static_cast<unsigned>(q >> 32);
+        int v = dest;
+        int steps = 0;
+        while (v != src) {
+          if (v < 0 || ++steps > n1) {
+            atomicOr(a.err, kErrWalk);
+            break;
+          }
+          // 64-bit total as two native 32-bit adds; a wrapped low word carries
+          unsigned* t32 = reinterpret_cast<unsigned*>(thr + v);
+          const unsigned old_lo = atomicAdd(t32, q_lo);
+          const unsigned carry = old_lo + q_lo < old_lo ? 1u : 0u;
+          if (q_hi | carry) atomicAdd(t32 + 1, q_hi + carry);
+          v = parent_of<COMPACT>(parent, par16, v);
+        }
       }
     }
     __syncthreads();
     unsigned long long* y = a.y_fx + static_cast<size_t>(scen) * a.g.m;
     for (int v = threadIdx.x; v < n1; v += BLOCK) {
-      const long long q = thr[v];
-      if (q != 0) atomicAdd(y + (COMPACT ? gslot[v] : pred[v]), static_cast<unsigned long long>(q));
+      if constexpr (COMPACT) {
+        const unsigned q = tot32[v];
+        if (q != 0u) atomicAdd(y + gslot[v], static_cast<unsigned long long>(q) << kshift);
+      } else {
+        const long long q = thr[v];
+        if (q != 0) atomicAdd(y + pred[v], static_cast<unsigned long long>(q));
+      }
     }
   }
 }
