@@ -339,11 +339,9 @@ __device__ __forceinline__ int relax_range(int src, int e0, int e1, int first_th
   return pushes;
 }
 
-__device__ __forceinline__ int warp_sum(int v) {
-#pragma unroll
-  for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
-  return v;
-}
+// sum over a converged warp, every lane receiving it (one warp-wide reduction
+// instruction on this architecture)
+__device__ __forceinline__ int warp_sum(int v) { return __reduce_add_sync(kFull, v); }
 
 constexpr long long kMaxIdlePolls = 1ll << 24;  // bound on one warp's idle polling
 constexpr int kMaxRestarts = 64;
