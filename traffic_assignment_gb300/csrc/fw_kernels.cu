@@ -838,14 +838,12 @@ __device__ __forceinline__ int relax_range_nfq(int src, int e0, int e1, int firs
         if (nb < old && !(h < first_thru && h != src)) {
           const unsigned bit = 1u << (h & 31);
           if (nb < thr_bits) {
-            if (!(vload(near + (h >> 5)) & bit)) {
-              const unsigned prev = atomicOr(near + (h >> 5), bit);
-              if (!(prev & bit)) {
-                ++pushes;
-                ring_push<BLOCK>(ring, qhead, qtail, h, err, ovf);
-              }
+            const unsigned prev = atomicOr(near + (h >> 5), bit);
+            if (!(prev & bit)) {
+              ++pushes;
+              ring_push<BLOCK>(ring, qhead, qtail, h, err, ovf);
             }
-          } else if (!(vload(far + (h >> 5)) & bit)) {
+          } else {
             atomicOr(far + (h >> 5), bit);
           }
         }
@@ -908,19 +906,19 @@ __device__ __forceinline__ void nfq_expand(const PathArgs& a, const uint2* e4s, 
           if (base + j >= deg) break;
           const int h = static_cast<int>(r4[j].x);
           const U nb = DT<T>::bits(DT<T>::add(du, __uint_as_float(r4[j].y)));
-          if (nb < vload(dist + h)) {
+          {  // the atomic alone: its returned value is the check
             const U old = atomicMin(dist + h, nb);
             if (nb < old && !(h < F && h != src)) {
               const unsigned bit = 1u << (h & 31);
               if (nb < thr) {
-                if (!(vload(near + (h >> 5)) & bit)) {
-                  const unsigned prev = atomicOr(near + (h >> 5), bit);
-                  if (!(prev & bit)) {
-                    ++pushes;
-                    ring_push<BLOCK>(ring, qhead, qtail, h, a.err, ovf);
-                  }
+                // no read-before-or either (the kernel is issue-bound: an atomic
+                // costs fewer issue slots than the check that would skip it)
+                const unsigned prev = atomicOr(near + (h >> 5), bit);
+                if (!(prev & bit)) {
+                  ++pushes;
+                  ring_push<BLOCK>(ring, qhead, qtail, h, a.err, ovf);
                 }
-              } else if (!(vload(far + (h >> 5)) & bit)) {
+              } else {
                 atomicOr(far + (h >> 5), bit);
               }
             }
