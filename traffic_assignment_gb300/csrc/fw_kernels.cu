@@ -873,13 +873,21 @@ __device__ __forceinline__ void nfq_expand(const PathArgs& a, const uint2* e4s, 
   uint2 r4[4];
   if (expand) {
     if constexpr (kPadded) {
-      deg = __ldg(a.g.out_deg + v);
+      // with 16-bit ring entries the degree rides in the upper half of the
+      // first record's head word (no separate load); else it is read apart
+      constexpr bool kDeg16 = std::is_same<R, unsigned short>::value;
+      constexpr unsigned kHead = kDeg16 ? 0xffffu : 0xffffffffu;
       const uint4* p = reinterpret_cast<const uint4*>(e4s + static_cast<size_t>(v) * 4);
       const uint4 q0 = __ldg(p), q1 = __ldg(p + 1);
-      r4[0] = make_uint2(q0.x, q0.y);
-      r4[1] = make_uint2(q0.z, q0.w);
-      r4[2] = make_uint2(q1.x, q1.y);
-      r4[3] = make_uint2(q1.z, q1.w);
+      if constexpr (kDeg16) {
+        deg = static_cast<int>(q0.x >> 16);
+      } else {
+        deg = __ldg(a.g.out_deg + v);
+      }
+      r4[0] = make_uint2(q0.x & kHead, q0.y);
+      r4[1] = make_uint2(q0.z & kHead, q0.w);
+      r4[2] = make_uint2(q1.x & kHead, q1.y);
+      r4[3] = make_uint2(q1.z & kHead, q1.w);
     } else {
       e0 = __ldg(a.g.row_ptr + v);
       deg = __ldg(a.g.row_ptr + v + 1) - e0;
@@ -1549,7 +1557,7 @@ __device__ __forceinline__ void write_weights(const LinkArgs& a, int scen, int k
     a.r32[i - k + __ldg(a.rpos + k)] = make_uint2(static_cast<unsigned>(__ldg(a.tail + k)), bits);
     if (a.e4) {
       const int p = __ldg(a.ell_pos + k);
-      if (p >= 0) a.e4[static_cast<size_t>(scen) * a.n1 * 4 + p] = rec;
+      if (p >= 0) a.e4[static_cast<size_t>(scen) * a.n1 * 4 + p] = make_uint2(__ldg(a.e4x + k), bits);
     }
   }
   if (a.w64) a.w64[i] = t;

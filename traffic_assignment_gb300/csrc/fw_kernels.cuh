@@ -119,6 +119,8 @@ struct LinkArgs {
   uint2* e32;                   // [S][m] packed fp32 edge records, or nullptr
   uint2* e4;                    // [S][n1][4] first four records of each node, or nullptr
   const int* ell_pos;           // [m] slot of link k in its tail's four (-1: beyond the fourth)
+  const unsigned* e4x;          // [m] first word of link k's padded record: its head, with the
+                                //     tail's out-degree in the upper 16 bits (16-bit queue ring)
   int n1;
   uint2* r32;                   // [S][m] packed fp32 reverse records (with e32)
   const int* head;              // [m] head node of each link (for e32)

@@ -190,6 +190,7 @@ LinkArgs Ctx::link_args(int nscen) const {
   a.r32 = fp64 ? nullptr : r32;
   a.e4 = fp64 ? nullptr : e4;
   a.ell_pos = ell_pos;
+  a.e4x = e4x;
   a.n1 = n1;
   a.head = head;
   a.tail = tail;
@@ -284,8 +285,9 @@ int Ctx::plan_launches() {
   sssp_variant = (opt.sssp_variant >= kSsspRounds && opt.sssp_variant <= kSsspNearFarQueue)
                      ? opt.sssp_variant
                      : kSsspNearFarQueue;
-  // the ring of the queue variant holds 16-bit node ids
-  if (sssp_variant == kSsspNearFarQueue && n1 > 0xffff) sssp_variant = kSsspNearFarQueueWide;
+  // the ring of the queue variant holds 16-bit node ids, and its padded
+  // records 16-bit heads and degrees
+  if (sssp_variant == kSsspNearFarQueue && !deg16) sssp_variant = kSsspNearFarQueueWide;
   const bool nf = sssp_variant == kSsspNearFar || sssp_variant == kSsspNearFarQueue ||
                   sssp_variant == kSsspNearFarQueueWide;
   sssp_block = opt.sssp_block > 0 ? opt.sssp_block : (nf ? 256 : 512);
@@ -628,6 +630,7 @@ static int create_impl(const tapgpu_network* net, const tapgpu_demand* dem,
   TG_TRY(c->alloc_n(&c->in_head, M));
   TG_TRY(c->alloc_n(&c->out_deg, n1));
   TG_TRY(c->alloc_n(&c->ell_pos, M));
+  TG_TRY(c->alloc_n(&c->e4x, M));
   TG_TRY(c->alloc_n(&c->rpos, M));
   TG_TRY(c->alloc_n(&c->fft, M));
   TG_TRY(c->alloc_n(&c->alpha, M));
@@ -649,8 +652,17 @@ static int create_impl(const tapgpu_network* net, const tapgpu_demand* dem,
       pos[k] = j < 4 ? v * 4 + j : -1;
     }
     c->h_ell_pos = pos;
+    int maxdeg = 0;
+    for (int v = 0; v < n1; ++v) maxdeg = std::max(maxdeg, deg[v]);
+    c->deg16 = n1 <= 0xffff && maxdeg <= 0xffff;
+    c->h_e4x.resize(M);
+    for (int k = 0; k < M; ++k) {
+      const unsigned h = static_cast<unsigned>(c->h_head[k]);
+      c->h_e4x[k] = c->deg16 ? h | (static_cast<unsigned>(deg[c->h_tail[k]]) << 16) : h;
+    }
     TG_CUDA(cudaMemcpy(c->out_deg, deg.data(), sizeof(int) * n1, cudaMemcpyHostToDevice));
     TG_CUDA(cudaMemcpy(c->ell_pos, pos.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
+    TG_CUDA(cudaMemcpy(c->e4x, c->h_e4x.data(), sizeof(unsigned) * M, cudaMemcpyHostToDevice));
   }
   TG_CUDA(cudaMemcpy(c->rpos, c->h_rpos.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
   TG_CUDA(cudaMemcpy(c->fft, c->h_fft.data(), sizeof(double) * M, cudaMemcpyHostToDevice));
@@ -1132,7 +1144,7 @@ static int to_device_weights(Ctx* c, const double* weights) {
                           c->stream));
   std::vector<uint2> w4(static_cast<size_t>(c->n1) * 4, make_uint2(0u, 0u));
   for (int k = 0; k < c->M; ++k)
-    if (c->h_ell_pos[k] >= 0) w4[c->h_ell_pos[k]] = wf[k];
+    if (c->h_ell_pos[k] >= 0) w4[c->h_ell_pos[k]] = make_uint2(c->h_e4x[k], wf[k].y);
   TG_CUDA(cudaMemcpyAsync(c->api_e4, w4.data(), sizeof(uint2) * w4.size(), cudaMemcpyHostToDevice,
                           c->stream));
   TG_CUDA(cudaStreamSynchronize(c->stream));

@@ -34,6 +34,9 @@ struct Ctx {
   int* in_head = nullptr;  // head node of each reverse-star slot
   int* out_deg = nullptr;  // out-degree of each node
   int* ell_pos = nullptr;  // slot of each link among its tail's first four (-1: beyond)
+  unsigned* e4x = nullptr;  // first word of each link's padded record (head | tail degree << 16)
+  std::vector<unsigned> h_e4x;
+  bool deg16 = false;       // node ids and out-degrees fit 16 bits (16-bit queue ring)
   std::vector<int> h_ell_pos;
   double *fft = nullptr, *alpha = nullptr, *beta = nullptr;
   unsigned char* ipow = nullptr;
