@@ -1400,17 +1400,18 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
     if (!a.do_load) continue;
     const int j0 = __ldg(a.dem.od_ptr + sidx), j1 = __ldg(a.dem.od_ptr + sidx + 1);
     const long long* oq = a.dem.od_q + scen * a.dem.q_stride;
-    // COMPACT (FP32 paths): 32-bit node totals in units of 2^kshift of the
+    // FP32 paths: 32-bit node totals in units of 2^kshift of the
     // fixed point, kshift the smallest that keeps this origin's whole demand
     // below 2^31, so that a walk step is one 32-bit add without a return
     // value.  Each OD demand is rounded to the nearest unit (for a 10k-node
     // network about 1e-6 trips; no bias, and the roundings of at most 2^31
     // OD pairs keep every total below 2^32): far inside the FP32-path
     // tolerance, and the sums stay exact integers, independent of order.
-    // Otherwise 64-bit totals.
+    // FP64 paths: 64-bit totals.
+    constexpr bool kWalk32 = std::is_same<T, float>::value;
     unsigned* tot32 = reinterpret_cast<unsigned*>(base);
     int kshift = 0;
-    if constexpr (COMPACT) {
+    if constexpr (kWalk32) {
       unsigned long long tq = 0;
       for (int j = j0 + threadIdx.x; j < j1; j += BLOCK)
         tq += static_cast<unsigned long long>(__ldg(oq + j));
@@ -1440,7 +1441,7 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
         a.err_info[1] = dest;
         continue;
       }
-      if constexpr (COMPACT) {
+      if constexpr (kWalk32) {
         const unsigned qk =
             static_cast<unsigned>(kshift ? (q + (1ull << (kshift - 1))) >> kshift : q);
         if (qk == 0) continue;  // below this task's unit
@@ -1475,9 +1476,10 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
     __syncthreads();
     unsigned long long* y = a.y_fx + static_cast<size_t>(scen) * a.g.m;
     for (int v = threadIdx.x; v < n1; v += BLOCK) {
-      if constexpr (COMPACT) {
+      if constexpr (kWalk32) {
         const unsigned q = tot32[v];
-        if (q != 0u) atomicAdd(y + gslot[v], static_cast<unsigned long long>(q) << kshift);
+        if (q != 0u)
+          atomicAdd(y + (COMPACT ? gslot[v] : pred[v]), static_cast<unsigned long long>(q) << kshift);
       } else {
         const long long q = thr[v];
         if (q != 0) atomicAdd(y + pred[v], static_cast<unsigned long long>(q));
