@@ -268,6 +268,24 @@ int Ctx::ensure_scenarios(int S) {
     TG_TRY(alloc_n(&lam_hist, static_cast<size_t>(S) * hist_cap));
   }
   S_cap = S;
+  // Unless the caller fixed the chunk, the label buffer grows to hold a whole
+  // batch's tasks (up to 16 GiB), so that an iteration runs one shortest-path
+  // and one loading launch instead of one per chunk, each with its tail.
+  if (opt.chunk_tasks <= 0 && dist) {
+    const int64_t tb = static_cast<int64_t>(n1) * (fp64 ? 8 : 4);
+    const int64_t want = std::min<int64_t>(std::max<int64_t>(1, (int64_t(16) << 30) / tb),
+                                           static_cast<int64_t>(S) * std::max(Z, 1));
+    if (want > dist_tasks) {
+      free_owned(this, dist);
+      dist = nullptr;
+      TG_TRY(alloc(&dist, static_cast<size_t>(tb) * static_cast<size_t>(want)));
+      dist_tasks = want;
+      if (pred_buf) {  // sized by the label buffer: made again on its next use
+        free_owned(this, pred_buf);
+        pred_buf = nullptr;
+      }
+    }
+  }
   if (gexec) {
     cudaGraphExecDestroy(gexec);
     gexec = nullptr;
