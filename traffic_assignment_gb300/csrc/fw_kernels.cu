@@ -909,28 +909,35 @@ __device__ __forceinline__ void nfq_expand(const PathArgs& a, const uint2* e4s, 
       // groups of four: the padded records first, then (degree > 4, rare on
       // road networks) the node's further CSR records in the same registers
       for (int base = 0;;) {
+        // the group's relaxations first, the ring appends of the heads that
+        // entered the near set after them: one copy of the append code, and
+        // a node enters the ring only once all its group's labels are set
+        // (fewer re-expansions)
+        unsigned pm = 0u;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           if (base + j >= deg) break;
           const int h = static_cast<int>(r4[j].x);
           const U nb = DT<T>::bits(DT<T>::add(du, __uint_as_float(r4[j].y)));
-          {  // the atomic alone: its returned value is the check
-            const U old = atomicMin(dist + h, nb);
-            if (nb < old && !(h < F && h != src)) {
-              const unsigned bit = 1u << (h & 31);
-              if (nb < thr) {
-                // no read-before-or either (the kernel is issue-bound: an atomic
-                // costs fewer issue slots than the check that would skip it)
-                const unsigned prev = atomicOr(near + (h >> 5), bit);
-                if (!(prev & bit)) {
-                  ++pushes;
-                  ring_push<BLOCK>(ring, qhead, qtail, h, a.err, ovf);
-                }
-              } else {
-                atomicOr(far + (h >> 5), bit);
-              }
+          // the atomic alone: its returned value is the check (the kernel is
+          // issue-bound: an atomic costs fewer issue slots than a
+          // read-before-atomic check that would skip it); likewise below
+          const U old = atomicMin(dist + h, nb);
+          if (nb < old && !(h < F && h != src)) {
+            const unsigned bit = 1u << (h & 31);
+            if (nb < thr) {
+              const unsigned prev = atomicOr(near + (h >> 5), bit);
+              if (!(prev & bit)) pm |= 1u << j;
+            } else {
+              atomicOr(far + (h >> 5), bit);
             }
           }
+        }
+        while (pm) {
+          const int j = __ffs(pm) - 1;
+          pm &= pm - 1;
+          ++pushes;
+          ring_push<BLOCK>(ring, qhead, qtail, static_cast<int>(r4[j].x), a.err, ovf);
         }
         base += 4;
         if (base >= deg) break;
