@@ -147,3 +147,34 @@ def test_demand_scenarios_argument_checks(built_lib):
         r = s.solve(max_iters=5)
         ref = oracle.frankwolfe(net, dem, threads=1, max_iters=5)
         assert _rel(s.flows()[0], ref["x"]) < 1e-6 and r["iterations"] == 5
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_label_buffer_grows_with_the_batch(built_lib, precision):
+    """The label buffer starts at 4,096 tasks per origin and grows when a batch
+    holds more: 4,100 scenarios of the 24-node network (98,400 tasks).  The
+    batched flows equal individual solves, and the one-shot shortest-path
+    entry point, whose predecessor buffer is re-made with the label buffer,
+    still matches the oracle afterwards."""
+    net, dem = synth.make_small24()
+    scen = synth.make_scenarios(net, 4100, seed=77)
+    pick = [0, 2049, 4099]
+    with Solver(net, dem, precision=precision) as s:
+        d0, p0 = s.sssp(net.fft, [1, 5, 24])
+        res = s.solve_scenarios(scen, max_iters=3)
+        assert all(r["error_bits"] == 0 and r["iterations"] == 3 for r in res)
+        batched = [s.flows(i)[0] for i in pick]
+        d1, p1 = s.sssp(net.fft, [1, 5, 24])
+    np.testing.assert_array_equal(d0, d1)
+    np.testing.assert_array_equal(p0, p1)
+    va, ea = net.csr()
+    dref, _ = oracle.sssp_all(va, ea, net.fft, net.num_nodes + 1, np.array([1, 5, 24]),
+                              net.first_thru_node)
+    np.testing.assert_array_equal(d1, dref)
+    for i, x in zip(pick, batched):
+        cap = net.capacity.copy()
+        cap[scen[i].links] = scen[i].new_capacity
+        with Solver(net, dem, precision=precision) as s1:
+            s1.set_capacity(cap)
+            s1.solve(max_iters=3)
+            np.testing.assert_array_equal(x, s1.flows()[0])
