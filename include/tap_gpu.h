@@ -281,6 +281,11 @@ int tapgpu_solve_begin(tapgpu_ctx *ctx, int max_iters, double target_relgap, con
 int tapgpu_solve_advance(tapgpu_ctx *ctx, int max_new_iters, int *done, tapgpu_result *res);
 /* volume and cost [M] of scenario s (0 for tapgpu_solve) */
 int tapgpu_get_link_flows(tapgpu_ctx *ctx, int scenario, double *volume, double *cost);
+/* volume and cost [count][M] of scenarios first .. first+count-1 in one call
+ * (either may be NULL).  No counterpart in the reference, whose scenario farm
+ * writes one flows file per solve; batched scenarios read back here at once. */
+int tapgpu_get_link_flows_batch(tapgpu_ctx *ctx, int first, int count, double *volume,
+                                double *cost);
 /* per-iteration rows of scenario s: rows[i*TAPGPU_TRACE_COLS + c] */
 int tapgpu_get_trace(tapgpu_ctx *ctx, int scenario, double *rows, int max_rows, int *nrows);
 /* replace the base capacities [M] */

@@ -178,3 +178,36 @@ def test_label_buffer_grows_with_the_batch(built_lib, precision):
             s1.set_capacity(cap)
             s1.solve(max_iters=3)
             np.testing.assert_array_equal(x, s1.flows()[0])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_scenario_edits_zero_repeated_and_batch_readback(built_lib, precision):
+    """Scenario capacity rows are made on the device from the base row and the
+    edits: a zero capacity takes the row's smallest positive capacity (the
+    zero-capacity fix-up), a link edited twice keeps its last value, and an
+    edit can itself be the new smallest capacity.  Each batched scenario
+    equals a solve with that capacity array; the batch read-back equals the
+    per-scenario one."""
+    net, dem = synth.make_grid416()
+    a, b = 3, 10
+    scen = [synth.Scenario("zero", np.array([a]), np.array([0.0])),
+            synth.Scenario("twice", np.array([b, a, b]), np.array([5.0, 7.0, 9000.0])),
+            synth.Scenario("smallest", np.array([a, b]), np.array([1e-3, 0.0]))]
+    with Solver(net, dem, precision=precision) as s:
+        res = s.solve_scenarios(scen, max_iters=5)
+        assert all(r["error_bits"] == 0 for r in res)
+        v, t = s.flows_batch()
+        single = [s.flows(i) for i in range(len(scen))]
+    for i in range(len(scen)):
+        np.testing.assert_array_equal(v[i], single[i][0])
+        np.testing.assert_array_equal(t[i], single[i][1])
+    for i, sc in enumerate(scen):
+        cap = net.capacity.copy()
+        for k, c in zip(sc.links, sc.new_capacity):
+            cap[k] = c
+        with Solver(net, dem, precision=precision) as s1:
+            s1.set_capacity(cap)
+            s1.solve(max_iters=5)
+            x1, t1 = s1.flows()
+        np.testing.assert_array_equal(v[i], x1)
+        np.testing.assert_array_equal(t[i], t1)

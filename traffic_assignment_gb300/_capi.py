@@ -77,8 +77,8 @@ EXPORTED = [
     "parse_flows_file", "parse_net_mod_file", "link_data_compar", "parse_trip_mod_file",
     "tapgpu_default_options", "tapgpu_status_string", "tapgpu_last_message", "tapgpu_create",
     "tapgpu_destroy", "tapgpu_solve", "tapgpu_solve_begin", "tapgpu_solve_advance",
-    "tapgpu_get_link_flows", "tapgpu_get_trace", "tapgpu_set_capacity",
-    "tapgpu_solve_scenarios", "tapgpu_sssp", "tapgpu_aon", "tapgpu_stream",
+    "tapgpu_get_link_flows", "tapgpu_get_link_flows_batch", "tapgpu_get_trace",
+    "tapgpu_set_capacity", "tapgpu_solve_scenarios", "tapgpu_sssp", "tapgpu_aon", "tapgpu_stream",
     "tapgpu_profile_iteration", "tapgpu_run_iterations", "tapgpu_set_timing",
     "tapgpu_get_timing", "tapgpu_get_path_stats", "tapgpu_sssp_labels_noalloc",
     "tapgpu_adjoint_vht", "tapgpu_get_tape", "tapgpu_set_scenario_demand",
@@ -116,6 +116,7 @@ def load(path: str | None = None):
     L.tapgpu_solve_begin.argtypes = [vp, C.c_int, C.c_double, F64P]
     L.tapgpu_solve_advance.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(Result)]
     L.tapgpu_get_link_flows.argtypes = [vp, C.c_int, F64P, F64P]
+    L.tapgpu_get_link_flows_batch.argtypes = [vp, C.c_int, C.c_int, F64P, F64P]
     L.tapgpu_get_trace.argtypes = [vp, C.c_int, F64P, C.c_int, C.POINTER(C.c_int)]
     L.tapgpu_set_capacity.argtypes = [vp, F64P]
     L.tapgpu_solve_scenarios.argtypes = [vp, C.c_int, I64P, I64P, F64P, C.c_int, C.c_double,
@@ -140,8 +141,8 @@ def load(path: str | None = None):
     L.tapgpu_set_scenario_demand.argtypes = [vp, C.c_int, F64P]
     L.tapgpu_set_scenario_demand.restype = C.c_int
     for fn in ("tapgpu_create", "tapgpu_solve", "tapgpu_solve_begin", "tapgpu_solve_advance",
-               "tapgpu_get_link_flows", "tapgpu_get_trace", "tapgpu_set_capacity",
-               "tapgpu_solve_scenarios", "tapgpu_sssp", "tapgpu_aon",
+               "tapgpu_get_link_flows", "tapgpu_get_link_flows_batch", "tapgpu_get_trace",
+               "tapgpu_set_capacity", "tapgpu_solve_scenarios", "tapgpu_sssp", "tapgpu_aon",
                "tapgpu_profile_iteration", "tapgpu_run_iterations", "tapgpu_set_timing",
                "tapgpu_get_timing"):
         getattr(L, fn).restype = C.c_int

@@ -2087,4 +2087,48 @@ cudaError_t launch_step(const LinkArgs& a, int grid, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// Scenario capacity rows made on the device: each row starts as the base
+// row (already positive), then one thread per scenario applies its edits in
+// their order, a non-positive value replaced by the scenario's smallest
+// positive capacity (the zero-capacity fix-up of
+// tap/tap_frankwolfe_pthread.c:654-669, computed on the host).
+__global__ void __launch_bounds__(kLinkBlock) k_scen_base_rows(double* cap, const double* base,
+                                                               int m) {
+  const size_t row = static_cast<size_t>(blockIdx.y) * m;
+  for (int k = blockIdx.x * kLinkBlock + threadIdx.x; k < m; k += gridDim.x * kLinkBlock)
+    cap[row + k] = base[k];
+}
+
+__global__ void __launch_bounds__(kLinkBlock) k_scen_edits(double* cap, int m, int nscen,
+                                                           const int* ptr, const int* link,
+                                                           const double* val,
+                                                           const double* min_pos) {
+  const int s = blockIdx.x * kLinkBlock + threadIdx.x;
+  if (s >= nscen) return;
+  double* row = cap + static_cast<size_t>(s) * m;
+  for (int i = ptr[s]; i < ptr[s + 1]; ++i) row[link[i]] = val[i] > 0 ? val[i] : min_pos[s];
+}
+
+// rows 1 .. nscen-1 of x [nscen][m] become copies of row 0
+__global__ void __launch_bounds__(kLinkBlock) k_replicate_rows(double* x, int m) {
+  const size_t row = static_cast<size_t>(blockIdx.y + 1) * m;
+  for (int k = blockIdx.x * kLinkBlock + threadIdx.x; k < m; k += gridDim.x * kLinkBlock)
+    x[row + k] = x[k];
+}
+
+cudaError_t launch_scenario_caps(double* cap, const double* base, int m, int nscen, const int* ptr,
+                                 const int* link, const double* val, const double* min_pos,
+                                 int grid, cudaStream_t s) {
+  k_scen_base_rows<<<dim3(grid, nscen), kLinkBlock, 0, s>>>(cap, base, m);
+  k_scen_edits<<<(nscen + kLinkBlock - 1) / kLinkBlock, kLinkBlock, 0, s>>>(cap, m, nscen, ptr, link,
+                                                                           val, min_pos);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_replicate_rows(double* x, int m, int nscen, int grid, cudaStream_t s) {
+  if (nscen < 2) return cudaSuccess;
+  k_replicate_rows<<<dim3(grid, nscen - 1), kLinkBlock, 0, s>>>(x, m);
+  return cudaGetLastError();
+}
+
 }  // namespace tapgpu

@@ -172,6 +172,12 @@ cudaError_t launch_set_costs(const LinkArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_ls_pass(const LinkArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_ls_fallback(const LinkArgs& a, cudaStream_t s);
 cudaError_t launch_step(const LinkArgs& a, int grid, cudaStream_t s);
+// capacity rows [nscen][m] = base with each scenario's edits (see fw_kernels.cu)
+cudaError_t launch_scenario_caps(double* cap, const double* base, int m, int nscen, const int* ptr,
+                                 const int* link, const double* val, const double* min_pos,
+                                 int grid, cudaStream_t s);
+// rows 1 .. nscen-1 of x [nscen][m] become copies of row 0
+cudaError_t launch_replicate_rows(double* x, int m, int nscen, int grid, cudaStream_t s);
 int sssp_occupancy(bool fp64, int block, bool smem, int n1, int variant);  // CTAs per SM
 int aon_occupancy(bool fp64, int block, bool smem, int n1);
 

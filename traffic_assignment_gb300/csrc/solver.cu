@@ -876,6 +876,7 @@ int tapgpu_set_capacity(tapgpu_ctx* ctx, const double* capacity) {
     const double v = capacity[c->perm[k]];
     c->h_cap[k] = v > 0 ? v : min_cap;
   }
+  c->base_dirty = true;
   TG_CUDA(cudaSetDevice(c->device));
   TG_CUDA(cudaMemcpy(c->cap, c->h_cap.data(), sizeof(double) * c->M, cudaMemcpyHostToDevice));
   return TAPGPU_OK;
@@ -961,6 +962,37 @@ int tapgpu_get_link_flows(tapgpu_ctx* ctx, int scenario, double* volume, double*
   return TAPGPU_OK;
 }
 
+int tapgpu_get_link_flows_batch(tapgpu_ctx* ctx, int first, int count, double* volume,
+                                double* cost) {
+  if (!ctx || count < 1) return TAPGPU_ERR_ARG;
+  Ctx* c = ctx->c;
+  if (first < 0 || first + count > c->S_cap) return TAPGPU_ERR_ARG;
+  TG_CUDA(cudaSetDevice(c->device));
+  TG_CUDA(cudaStreamSynchronize(c->stream));
+  const int M = c->M;
+  const size_t off = static_cast<size_t>(first) * M, n = static_cast<size_t>(count) * M;
+  bool identity = true;
+  for (int k = 0; k < M && identity; ++k) identity = c->perm[k] == k;
+  double* outs[2] = {volume, cost};
+  const double* srcs[2] = {c->x + off, c->t + off};
+  std::vector<double> tmp;
+  for (int a = 0; a < 2; ++a) {
+    if (!outs[a]) continue;
+    if (identity) {  // the caller's link order is the device's: one copy
+      TG_CUDA(cudaMemcpy(outs[a], srcs[a], sizeof(double) * n, cudaMemcpyDeviceToHost));
+      continue;
+    }
+    tmp.resize(n);
+    TG_CUDA(cudaMemcpy(tmp.data(), srcs[a], sizeof(double) * n, cudaMemcpyDeviceToHost));
+    for (int s = 0; s < count; ++s) {
+      const double* row = tmp.data() + static_cast<size_t>(s) * M;
+      double* out = outs[a] + static_cast<size_t>(s) * M;
+      for (int k = 0; k < M; ++k) out[c->perm[k]] = row[k];
+    }
+  }
+  return TAPGPU_OK;
+}
+
 int tapgpu_get_trace(tapgpu_ctx* ctx, int scenario, double* rows, int max_rows, int* nrows) {
   if (!ctx || !rows || !nrows) return TAPGPU_ERR_ARG;
   Ctx* c = ctx->c;
@@ -1005,23 +1037,79 @@ int tapgpu_solve_scenarios(tapgpu_ctx* ctx, int num_scen, const int64_t* scen_pt
   TG_TRY(c->ensure_scenarios(num_scen));
   c->use_dem_scen = c->dem_scen == num_scen;
   c->last_nscen = num_scen;
-  // capacities of every scenario: base with the scenario's edits
-  std::vector<double> caps(static_cast<size_t>(num_scen) * M);
-  for (int s = 0; s < num_scen; ++s) {
-    double* row = caps.data() + static_cast<size_t>(s) * M;
-    std::copy(c->h_cap.begin(), c->h_cap.end(), row);
-    for (int64_t i = scen_ptr[s]; i < scen_ptr[s + 1]; ++i) {
-      const double v = scen_cap[i];
-      row[inv[scen_links[i]]] = v;
-    }
-    double mn = DBL_MAX;
-    for (int k = 0; k < M; ++k)
-      if (row[k] > 0 && row[k] < mn) mn = row[k];
-    for (int k = 0; k < M; ++k)
-      if (!(row[k] > 0)) row[k] = mn;
+  // capacities of every scenario, made on the device from the base row and
+  // the edits; the host finds each scenario's smallest positive capacity
+  // for the zero-capacity fix-up
+  if (c->base_dirty) {
+    if (!c->base_cap) TG_TRY(c->alloc_n(&c->base_cap, M));
+    TG_CUDA(cudaMemcpy(c->base_cap, c->h_cap.data(), sizeof(double) * M, cudaMemcpyHostToDevice));
+    c->h_cap_order.resize(M);
+    std::iota(c->h_cap_order.begin(), c->h_cap_order.end(), 0);
+    std::stable_sort(c->h_cap_order.begin(), c->h_cap_order.end(),
+                     [c](int a, int b) { return c->h_cap[a] < c->h_cap[b]; });
+    c->base_dirty = false;
   }
-  TG_CUDA(cudaMemcpyAsync(c->cap, caps.data(), sizeof(double) * caps.size(),
+  const int64_t nedit = scen_ptr[num_scen] - scen_ptr[0];
+  std::vector<int> eptr(num_scen + 1), elink(static_cast<size_t>(std::max<int64_t>(nedit, 1)));
+  std::vector<double> evalv(elink.size()), emin(num_scen);
+  {
+    std::vector<int> seen;  // links edited in this scenario (few)
+    int64_t j = 0;
+    for (int s = 0; s < num_scen; ++s) {
+      eptr[s] = static_cast<int>(j);
+      seen.clear();
+      for (int64_t i = scen_ptr[s]; i < scen_ptr[s + 1]; ++i, ++j) {
+        elink[j] = static_cast<int>(inv[scen_links[i]]);
+        evalv[j] = scen_cap[i];
+        seen.push_back(elink[j]);
+      }
+      // smallest positive capacity of the final row: edits (the last edit of
+      // a link wins) and the smallest base capacity of a link not edited
+      double mn = DBL_MAX;
+      for (int64_t i = eptr[s]; i < j; ++i) {
+        bool last = true;
+        for (int64_t i2 = i + 1; i2 < j; ++i2) last = last && elink[i2] != elink[i];
+        if (last && evalv[i] > 0 && evalv[i] < mn) mn = evalv[i];
+      }
+      for (int k : c->h_cap_order) {
+        if (std::find(seen.begin(), seen.end(), k) != seen.end()) continue;
+        if (c->h_cap[k] < mn) mn = c->h_cap[k];
+        break;
+      }
+      emin[s] = mn;
+    }
+    eptr[num_scen] = static_cast<int>(j);
+  }
+  if (num_scen + 1 > c->ed_scen_cap) {
+    if (c->ed_ptr) tapgpu::free_owned(c, c->ed_ptr);
+    if (c->ed_min) tapgpu::free_owned(c, c->ed_min);
+    c->ed_ptr = nullptr;
+    c->ed_min = nullptr;
+    TG_TRY(c->alloc_n(&c->ed_ptr, num_scen + 1));
+    TG_TRY(c->alloc_n(&c->ed_min, num_scen + 1));
+    c->ed_scen_cap = num_scen + 1;
+  }
+  if (static_cast<int64_t>(elink.size()) > c->ed_cap) {
+    if (c->ed_link) tapgpu::free_owned(c, c->ed_link);
+    if (c->ed_val) tapgpu::free_owned(c, c->ed_val);
+    c->ed_link = nullptr;
+    c->ed_val = nullptr;
+    TG_TRY(c->alloc_n(&c->ed_link, elink.size()));
+    TG_TRY(c->alloc_n(&c->ed_val, elink.size()));
+    c->ed_cap = static_cast<int64_t>(elink.size());
+  }
+  TG_CUDA(cudaMemcpyAsync(c->ed_ptr, eptr.data(), sizeof(int) * eptr.size(),
                           cudaMemcpyHostToDevice, c->stream));
+  TG_CUDA(cudaMemcpyAsync(c->ed_link, elink.data(), sizeof(int) * elink.size(),
+                          cudaMemcpyHostToDevice, c->stream));
+  TG_CUDA(cudaMemcpyAsync(c->ed_val, evalv.data(), sizeof(double) * evalv.size(),
+                          cudaMemcpyHostToDevice, c->stream));
+  TG_CUDA(cudaMemcpyAsync(c->ed_min, emin.data(), sizeof(double) * emin.size(),
+                          cudaMemcpyHostToDevice, c->stream));
+  TG_CUDA(tapgpu::launch_scenario_caps(c->cap, c->base_cap, M, num_scen, c->ed_ptr, c->ed_link,
+                                       c->ed_val, c->ed_min, c->link_grid, c->stream));
+  // the host vectors above must outlive the copies
+  TG_CUDA(cudaStreamSynchronize(c->stream));
   std::vector<int> all(num_scen);
   std::iota(all.begin(), all.end(), 0);
   TG_CUDA(cudaMemcpyAsync(c->scen_list, all.data(), sizeof(int) * num_scen,
@@ -1029,11 +1117,11 @@ int tapgpu_solve_scenarios(tapgpu_ctx* ctx, int num_scen, const int64_t* scen_pt
   c->h_scen_list = all;
   TG_TRY(tapgpu::upload_states(c, num_scen, max_iters, target_relgap));
   if (x0) {
+    // the warm start once, then copied to every scenario on the device
     std::vector<double> xi(M);
     for (int k = 0; k < M; ++k) xi[k] = x0[c->perm[k]];
-    for (int s = 0; s < num_scen; ++s)
-      TG_CUDA(cudaMemcpyAsync(c->x + static_cast<size_t>(s) * M, xi.data(), sizeof(double) * M,
-                              cudaMemcpyHostToDevice, c->stream));
+    TG_CUDA(cudaMemcpyAsync(c->x, xi.data(), sizeof(double) * M, cudaMemcpyHostToDevice, c->stream));
+    TG_CUDA(tapgpu::launch_replicate_rows(c->x, M, num_scen, c->link_grid, c->stream));
     TG_CUDA(cudaStreamSynchronize(c->stream));
     TG_TRY(c->enqueue_initial(num_scen, true));
   } else if (c->use_dem_scen) {

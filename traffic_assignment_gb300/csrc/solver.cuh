@@ -28,6 +28,17 @@ struct Ctx {
   std::vector<int64_t> perm;  // internal link k -> caller's link index
   std::vector<int> h_tail, h_head;
   std::vector<double> h_cap, h_fft, h_alpha, h_beta;
+  // base capacities on the device for the scenario rows, and the links in
+  // order of increasing base capacity (both redone after tapgpu_set_capacity)
+  double* base_cap = nullptr;
+  std::vector<int> h_cap_order;
+  bool base_dirty = true;
+  // per-call scenario edits on the device (grown as needed)
+  int* ed_ptr = nullptr;
+  int* ed_link = nullptr;
+  double* ed_val = nullptr;
+  double* ed_min = nullptr;
+  int64_t ed_scen_cap = 0, ed_cap = 0;
 
   // device topology and link parameters
   int *row_ptr = nullptr, *head = nullptr, *tail = nullptr, *in_ptr = nullptr, *in_link = nullptr;

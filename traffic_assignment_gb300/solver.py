@@ -81,6 +81,7 @@ class Solver:
         opt.line_search = {"reference": 0, "exact": 1}[line_search]
         opt.tape_checkpoint = int(tape_checkpoint)
         self.precision = "fp32" if opt.precision == K.TAPGPU_FP32_PATHS else "fp64"
+        self.last_scenarios = 1
         keep: list = []
         ns = _net_struct(net, keep)
         ds = _dem_struct(dem, keep) if dem is not None else None
@@ -133,6 +134,17 @@ class Solver:
         v = np.zeros(self.m)
         t = np.zeros(self.m)
         K.check(self.L.tapgpu_get_link_flows(self.h, scenario, K.ptr(v, K.F64P), K.ptr(t, K.F64P)))
+        return v, t
+
+    def flows_batch(self, first: int = 0, count: Optional[int] = None):
+        """Volumes and costs [count][m] of scenarios first .. first+count-1 (of the
+        last solve_scenarios call by default: all of them) in one call."""
+        if count is None:
+            count = self.last_scenarios - first
+        v = np.zeros((count, self.m))
+        t = np.zeros((count, self.m))
+        K.check(self.L.tapgpu_get_link_flows_batch(self.h, first, count, K.ptr(v, K.F64P),
+                                                   K.ptr(t, K.F64P)))
         return v, t
 
     def trace(self, scenario: int = 0, max_rows: int = 1000000) -> np.ndarray:
@@ -192,6 +204,7 @@ class Solver:
                                               K.ptr(la, K.I64P), K.ptr(ca, K.F64P),
                                               int(max_iters), float(target_relgap),
                                               None if xa is None else K.ptr(xa, K.F64P), res))
+        self.last_scenarios = len(scenarios)
         return [SolveResult(r.as_dict()) for r in res]
 
     def adjoint_vht(self, scenario: int = 0):
