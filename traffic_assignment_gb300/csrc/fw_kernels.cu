@@ -1236,9 +1236,9 @@ __device__ __forceinline__ int parent_of(const int* parent, const unsigned short
 }
 
 // COMPACT (FP32 labels, at most 65535 nodes): 8 bytes per node hold the
-// labels and the predecessor search, then the 64-bit node totals; parents
-// are 16-bit and the predecessor links move to the task's slot of the label
-// buffer (its labels are in shared memory by then).  10 bytes per node let
+// labels and the predecessor words, the labels' half later the 32-bit node
+// totals; parents are 16-bit (the task's slot of the label buffer serves as
+// scratch once its labels are in shared memory).  10 bytes per node let
 // two CTAs share an SM up to ~11,500 nodes, so that one task's longest walks
 // overlap another task's work.  Otherwise 16 bytes per node: totals (labels
 // first), predecessor links, parents.
@@ -1274,7 +1274,7 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
     const Edges<T> ed = edges_of<T>(a, scen);
     const RevEdges<T> rv = rev_edges_of<T>(a, scen);
     const T* din = static_cast<const T*>(a.dist) + static_cast<size_t>(task - a.task_begin) * n1;
-    // COMPACT: the slot's labels are copied below; it then holds scratch and the links
+    // COMPACT: the slot's labels are copied below; it then serves as scratch
     int* gslot = reinterpret_cast<int*>(const_cast<T*>(din));
     int* scr = COMPACT ? gslot : parent;
 
@@ -1391,7 +1391,6 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
       if constexpr (COMPACT) {
         par16[v] = ok ? static_cast<unsigned short>(pack ? (p & 0xffffu) : __ldg(a.g.tail + p))
                       : kNoParent16;
-        gslot[v] = ok ? static_cast<int>(pack ? p >> 16 : p) : -1;
       } else {
         parent[v] = ok ? __ldg(a.g.tail + p) : -1;
       }
@@ -1484,9 +1483,14 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
     unsigned long long* y = a.y_fx + static_cast<size_t>(scen) * a.g.m;
     for (int v = threadIdx.x; v < n1; v += BLOCK) {
       if constexpr (kWalk32) {
+        // the 32-bit totals cover the labels only: the predecessor words
+        // (the link, packed with the tail in the compact layout) are intact
         const unsigned q = tot32[v];
-        if (q != 0u)
-          atomicAdd(y + (COMPACT ? gslot[v] : pred[v]), static_cast<unsigned long long>(q) << kshift);
+        if (q != 0u) {
+          const unsigned pw = up[v];
+          const unsigned k = COMPACT && pack ? pw >> 16 : pw;
+          atomicAdd(y + k, static_cast<unsigned long long>(q) << kshift);
+        }
       } else {
         const long long q = thr[v];
         if (q != 0) atomicAdd(y + pred[v], static_cast<unsigned long long>(q));
