@@ -7,8 +7,9 @@ grid + 200 two-way arterials, 40,000 links, 1,000 zones, gravity demand of
 scenarios in one batched launch sequence (FP32 path costs, FP64 gap /
 objective / line search / VHT).  ``value`` is scenario-iterations per second
 with everything resident in HBM; ``e2e`` is the same metric through the C ABI
-call tapgpu_solve_scenarios from host buffers (capacities and warm-start
-flows in, every scenario's flows and costs out).
+from host buffers: tapgpu_solve_scenarios (the scenarios' capacity edits and
+the warm-start flows in; the capacity rows are made on the device) and
+tapgpu_get_link_flows_batch (every scenario's flows and costs out).
 
 Also reported: scenarios/sec to relative gap 1e-4 for the batched solver and
 for the plain single-scenario GPU path, the roofline of the dominant kernel
