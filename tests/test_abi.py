@@ -175,3 +175,28 @@ def test_oracle_no_path_reported():
     net, dem = synth.make_grid416(first_thru_node=39)
     with pytest.raises(RuntimeError, match="rc=2"):
         oracle.frankwolfe(net, dem, threads=1, max_iters=2)
+
+
+def test_bench_counts_the_scenario_state_size(tmp_path):
+    """bench.py counts host-to-device bytes with the size of the device's
+    per-scenario state record: compile a host program against the header."""
+    import importlib.util
+    import shutil
+    import subprocess
+
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc absent")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = tmp_path / "sz.cu"
+    src.write_text('#include <cstdio>\n#include "fw_kernels.cuh"\n'
+                   'int main() { std::printf("%zu", sizeof(tapgpu::ScenState)); return 0; }\n')
+    exe = tmp_path / "sz"
+    subprocess.run([nvcc, "-std=c++17", "-I", os.path.join(root, "include"), "-I",
+                    os.path.join(root, "traffic_assignment_gb300", "csrc"), str(src), "-o", str(exe)],
+                   check=True, capture_output=True)
+    size = int(subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout)
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(root, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    assert bench.SCEN_STATE_BYTES == size
