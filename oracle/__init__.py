@@ -271,8 +271,9 @@ def ref_sssp(va, ea, wa, num_nodes1, source, first_thru, fn="sssp_pape_lll"):
 
 
 def run_reference(net, dem, threads=1, iters=0, relgap=0.0, warm_flows=None,
-                  binary="tap_frankwolfe_pthread", workdir=None):
-    """Run the compiled reference CLI on TNTP files written from (net, dem).
+                  binary="tap_frankwolfe_pthread", workdir=None, trip_mods=None):
+    """Run the compiled reference CLI on TNTP files written from (net, dem)
+    (``trip_mods``: a trip modifications file for its ``-t`` flag).
 
     Returns dict(volume, cost, header, log) where ``log`` rows are
     (iter, objective, relgap, avg_excess, total_cost) from the ``-v`` lines.
@@ -296,6 +297,8 @@ def run_reference(net, dem, threads=1, iters=0, relgap=0.0, warm_flows=None,
             cmd += ["-r", repr(relgap)]
         if warm_flows is not None:
             cmd += ["-w", warm_flows]
+        if trip_mods is not None:
+            cmd += ["-t", trip_mods]
     else:
         cmd += ["-i", str(iters)] if iters else []
         cmd += ["-r", repr(relgap)] if relgap else []

@@ -8,6 +8,9 @@ compressed .npz files:
   fw_<case>.npz    network + demand, then the reference's flows / costs as
                    printed (%.15f), the flows-file header and every ``-v``
                    iteration line (objective, relgap, average excess, VHT)
+  tripmods_<case>.npz  the same with a trip modifications file (-t): the
+                   base demand and the modifications (kind, origin, dest,
+                   multiplier, in file order)
   sssp_<case>.npz  forward star, weights, and for every source the labels and
                    predecessor links of sssp_pape_lll (tap/sssp_pape.c:284)
 
@@ -33,7 +36,7 @@ OUT = os.path.dirname(os.path.abspath(__file__))
 REF_SSSP_DIR = "/root/reference/trunk/cuda_sssp"
 
 
-def _save_fw(name, net, dem, r, extra=None):
+def _save_fw(name, net, dem, r, extra=None, prefix="fw"):
     arrs = dict(
         num_nodes=net.num_nodes, num_zones=net.num_zones, first_thru_node=net.first_thru_node,
         init=net.init, term=net.term, capacity=net.capacity, length=net.length, fft=net.fft,
@@ -45,7 +48,7 @@ def _save_fw(name, net, dem, r, extra=None):
         hdr_totalcost=r["header"].get("totalcost", np.nan))
     if extra:
         arrs.update(extra)
-    np.savez_compressed(os.path.join(OUT, f"fw_{name}.npz"), **arrs)
+    np.savez_compressed(os.path.join(OUT, f"{prefix}_{name}.npz"), **arrs)
     print("wrote", name, "iters", arrs["hdr_iterations"], "relgap", arrs["hdr_relgap"])
 
 
@@ -71,6 +74,27 @@ def fw_cases():
     thru, dthru = synth.make_grid416_centroids()
     _save_fw("centroids454_i50", thru, dthru,
              oracle.run_reference(thru, dthru, threads=1, iters=50))
+
+
+def tripmod_cases():
+    """The reference's -t flag (tap/tap_main.c, tap/tap_functions.c:521-598):
+    one modification of each kind, applied in file order, then 60 iterations."""
+    from traffic_assignment_gb300 import tripmods
+    net, dem = synth.make_grid416()
+    o1 = 3
+    d1 = int(dem.od_dest[dem.od_ptr[o1]])  # an OD pair that exists
+    mods = [tripmods.TripMod("p2p", "P2P", o1, d1, 1.75),
+            tripmods.TripMod("orig", "UNIFORM", 5, 0, 0.6),
+            tripmods.TripMod("dest", "UNIFORM", 0, 12, 1.4),
+            tripmods.TripMod("all", "ALL", 0, 0, 1.05)]
+    wd = tempfile.mkdtemp(prefix="golden_")
+    path = os.path.join(wd, "tripmods.txt")
+    tripmods.write_trip_mods(path, mods)
+    r = oracle.run_reference(net, dem, threads=1, iters=60, workdir=wd, trip_mods=path)
+    _save_fw("grid416_i60", net, dem, r, extra=dict(
+        mod_kind=np.array([m.kind for m in mods]), mod_origin=np.array([m.origin for m in mods]),
+        mod_dest=np.array([m.dest for m in mods]),
+        mod_mult=np.array([m.multiplier for m in mods])), prefix="tripmods")
 
 
 def _read_rmat(path):
@@ -114,4 +138,5 @@ if __name__ == "__main__":
     if not oracle.reference_available():
         sys.exit("reference sources not available: cannot generate golden fixtures")
     fw_cases()
+    tripmod_cases()
     sssp_cases()

@@ -259,3 +259,21 @@ def test_link_array_operations(built_lib, tmp_path):
     lib.line_search.restype = C.c_double
     lam = lib.line_search(C.byref(nd), x.ctypes.data_as(F64P), d.ctypes.data_as(F64P))
     assert lam == oracle.line_search(net, x, d)
+
+
+def test_cli_trip_mods_match_reference_golden(built_lib, tmp_path):
+    """-t (trip modifications, tap/tap_main.c) against the reference's own run
+    with the same file: flows, costs and log lines within 1e-6."""
+    from test_oracle import load_tripmods_golden
+    from traffic_assignment_gb300 import tripmods
+    net, dem, mods, z = load_tripmods_golden()
+    nf, tf = _write_case(net, dem, str(tmp_path))
+    mf = os.path.join(str(tmp_path), "tripmods.txt")
+    tripmods.write_trip_mods(mf, mods)
+    _, _, vol, cost, hdr, log = _run_cli(["-n", "4", "-v", "-i", "60", "-t", mf, nf, tf])
+    assert _rel(vol, z["volume"]) < 1e-6
+    assert _rel(cost, z["cost"]) < 1e-6
+    assert int(hdr["iterations"]) == 60
+    assert abs(hdr["relgap"] - float(z["hdr_relgap"])) <= 1e-6 * abs(float(z["hdr_relgap"]))
+    for col in (1, 2, 4):
+        np.testing.assert_allclose(log[:, col], z["log"][:, col], rtol=1e-6)

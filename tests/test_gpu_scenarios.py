@@ -211,3 +211,20 @@ def test_scenario_edits_zero_repeated_and_batch_readback(built_lib, precision):
             x1, t1 = s1.flows()
         np.testing.assert_array_equal(v[i], x1)
         np.testing.assert_array_equal(t[i], t1)
+
+
+def test_demand_scenario_matches_reference_trip_mods_golden(built_lib):
+    """The reference's -t run as a demand scenario of the batched solver (FP64):
+    flows, costs and VHT within 1e-6 of the reference's own output."""
+    from test_oracle import load_tripmods_golden
+    from traffic_assignment_gb300 import tripmods
+    net, dem, mods, z = load_tripmods_golden()
+    with Solver(net, dem, precision="fp64") as s:
+        s.set_scenario_demand(tripmods.demand_scenarios(dem, [mods]))
+        res = s.solve_scenarios([synth.Scenario("base", np.zeros(0, np.int64), np.zeros(0))],
+                                max_iters=60)
+        x, t = s.flows(0)
+    assert res[0]["error_bits"] == 0 and res[0]["iterations"] == 60
+    assert _rel(x, z["volume"]) < 1e-6
+    assert _rel(t, z["cost"]) < 1e-6
+    assert abs(res[0]["total_cost"] - float(z["hdr_totalcost"])) <= 1e-6 * float(z["hdr_totalcost"])

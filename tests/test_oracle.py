@@ -124,3 +124,34 @@ def test_oracle_sssp_chicago_regional():
         dr, pr = oracle.ref_sssp(va, b, w, n1, int(s), 1)
         np.testing.assert_array_equal(d[i], dr)
         np.testing.assert_array_equal(p[i], pr)
+
+
+TRIPMODS = os.path.join(os.path.dirname(__file__), "golden", "tripmods_grid416_i60.npz")
+
+
+def load_tripmods_golden(path=TRIPMODS):
+    """Network, base demand, the trip modifications in file order, fixture."""
+    from traffic_assignment_gb300 import tripmods
+    net, dem, z = load_fw_golden(path)
+    mods = [tripmods.TripMod(f"m{i}", str(k), int(o), int(d), float(m))
+            for i, (k, o, d, m) in enumerate(zip(z["mod_kind"], z["mod_origin"], z["mod_dest"],
+                                                  z["mod_mult"]))]
+    return net, dem, mods, z
+
+
+def test_oracle_with_trip_mods_matches_reference_golden():
+    """The reference's -t run (one modification of each kind): the restated
+    modifications (traffic_assignment_gb300/tripmods.py) and the oracle give
+    the reference's printed flows, costs and log lines; without them the
+    answer differs."""
+    from traffic_assignment_gb300 import tripmods
+    net, dem, mods, z = load_tripmods_golden()
+    r = oracle.frankwolfe(net, tripmods.apply_trip_mods(dem, mods), threads=1, max_iters=60)
+    assert r["iterations"] == int(z["hdr_iterations"]) == 60
+    np.testing.assert_array_equal(fmt(r["x"]), fmt(z["volume"]))
+    np.testing.assert_array_equal(fmt(r["t"]), fmt(z["cost"]))
+    for col_ref, col_port in ((1, 0), (2, 1), (3, 2), (4, 3)):
+        np.testing.assert_array_equal(fmt(r["trace"][:, col_port]), fmt(z["log"][:, col_ref]))
+    assert "%.15f" % r["relgap"] == "%.15f" % float(z["hdr_relgap"])
+    base = oracle.frankwolfe(net, dem, threads=1, max_iters=60)
+    assert not np.array_equal(fmt(base["x"]), fmt(z["volume"]))
