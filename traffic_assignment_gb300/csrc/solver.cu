@@ -966,7 +966,7 @@ int tapgpu_get_link_flows_batch(tapgpu_ctx* ctx, int first, int count, double* v
                                 double* cost) {
   if (!ctx || count < 1) return TAPGPU_ERR_ARG;
   Ctx* c = ctx->c;
-  if (first < 0 || first + count > c->S_cap) return TAPGPU_ERR_ARG;
+  if (first < 0 || static_cast<int64_t>(first) + count > c->S_cap) return TAPGPU_ERR_ARG;
   TG_CUDA(cudaSetDevice(c->device));
   TG_CUDA(cudaStreamSynchronize(c->stream));
   const int M = c->M;
