@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <limits>
 #include <numeric>
 
 namespace tapgpu {
@@ -1050,6 +1051,10 @@ int tapgpu_solve_scenarios(tapgpu_ctx* ctx, int num_scen, const int64_t* scen_pt
     c->base_dirty = false;
   }
   const int64_t nedit = scen_ptr[num_scen] - scen_ptr[0];
+  if (nedit > std::numeric_limits<int>::max() - 1) {
+    tapgpu::set_message("too many scenario edits in one call");
+    return TAPGPU_ERR_ARG;
+  }
   std::vector<int> eptr(num_scen + 1), elink(static_cast<size_t>(std::max<int64_t>(nedit, 1)));
   std::vector<double> evalv(elink.size()), emin(num_scen);
   {
