@@ -371,16 +371,21 @@ int tapgpu_get_path_stats(tapgpu_ctx *ctx, int64_t *out);
  * can cause is not acceptable in their loop).  Every argument is device
  * memory owned by the caller: the forward star row_ptr[num_nodes1+1] /
  * head[num_links] (num_nodes1 counts node 0), link costs weight[num_links]
- * (finite, >= 0), sources[num_sources], and the output
- * dist[num_sources][num_nodes1] (+inf where unreachable).  Nodes below
- * first_thru_node are only expanded as sources.  The only other memory used
- * is a fixed 32 MiB array inside the library (a 256-byte control block plus
- * per-CTA label slices of 8*num_nodes1 + num_nodes1/4 bytes): larger graphs
- * are rejected with TAPGPU_ERR_UNSUPPORTED.  The first call on a device looks
- * up that array's device address; make it before any stream capture.  All
- * calls share the array, so calls that overlap on the GPU (other streams,
- * other host threads) race; serialise them.  Runs on `stream` (a
- * cudaStream_t, NULL for the default stream) and returns after it finishes. */
+ * (>= 0), sources[num_sources], and the output dist[num_sources][num_nodes1]
+ * (+inf where unreachable).  Nodes below first_thru_node are only expanded as
+ * sources.  The inputs are checked on the device before use (row_ptr
+ * non-decreasing within 0..num_links, heads and sources in 0..num_nodes1-1,
+ * weights >= 0); a failed check returns TAPGPU_ERR_ARG and leaves dist
+ * untouched.  The only other memory used is a fixed 32 MiB array inside the
+ * library (a 256-byte control block plus per-CTA label slices of
+ * 8*num_nodes1 + num_nodes1/4 bytes, rounded up to 16): num_nodes1 above
+ * 4,067,172 is rejected with TAPGPU_ERR_UNSUPPORTED before any CUDA call.
+ * Each call looks up the array's device address with the current device;
+ * the first call on a device also loads the library's device code there, so
+ * make it before any stream capture.  All calls share the array, so calls
+ * that overlap on the GPU (other streams, other host threads) race;
+ * serialise them.  Runs on `stream` (a cudaStream_t, NULL for the default
+ * stream) and returns after it finishes. */
 int tapgpu_sssp_labels_noalloc(int32_t num_nodes1, int32_t num_links, int32_t first_thru_node,
                                const int32_t *row_ptr, const int32_t *head, const double *weight,
                                const int32_t *sources, int32_t num_sources, double *dist,

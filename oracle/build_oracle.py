@@ -4,7 +4,8 @@
   (``oracle_tap.c``) into ``oracle/_build/liboracle_tap.so``.  It runs on any
   machine with gcc, including the GPU host, where it is rebuilt from source.
 * ``build_reference()`` compiles the reference's own CPU solver from the
-  sources where they lie under ``/root/reference/trunk/tap`` into
+  sources where they lie under ``$TAP_REFERENCE_ROOT/trunk/tap`` (the
+  reference checkout; default ``/root/reference``) into
   ``oracle/_ref/`` (never copying a source file), with the reference's flags
   (tap/common.mk:50 ``-O3 -fno-associative-math`` plus ``-pthread``):
 
@@ -26,7 +27,10 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REF_TAP = "/root/reference/trunk/tap"
+# the reference checkout: one setting for every recipe and test that reads it
+REFERENCE_ROOT = os.environ.get("TAP_REFERENCE_ROOT", "/root/reference")
+REF_TRUNK = os.path.join(REFERENCE_ROOT, "trunk")
+REF_TAP = os.path.join(REF_TRUNK, "tap")
 CFLAGS = ["-O3", "-fno-associative-math", "-pthread", "-DUNIX"]
 
 

@@ -33,7 +33,7 @@ import oracle  # noqa: E402
 from traffic_assignment_gb300 import synth, tntp  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
-REF_SSSP_DIR = "/root/reference/trunk/cuda_sssp"
+REF_SSSP_DIR = os.path.join(oracle.build_oracle.REF_TRUNK, "cuda_sssp")
 
 
 def _save_fw(name, net, dem, r, extra=None, prefix="fw"):

@@ -200,3 +200,19 @@ def test_bench_counts_the_scenario_state_size(tmp_path):
     bench = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(bench)
     assert bench.SCEN_STATE_BYTES == size
+
+
+# num_nodes1 (node 0 counted) whose FP64 labels and bitmaps still fit one
+# per-CTA slice of the allocation-free entry point's fixed 32 MiB array
+NOALLOC_MAX_NODES1 = 4_067_172
+
+
+def test_noalloc_size_limit_is_exact(lib):
+    """The allocation-free entry point applies its size limit before any CUDA
+    call: one node over the limit is refused, the limit itself passes the size
+    check (with no sources the call then returns without touching the GPU)."""
+    dummy = C.c_void_p(16)  # never dereferenced: the calls return before any device work
+    args = (0, 1, dummy, dummy, dummy, dummy, 0, None, None)
+    rc = lib.tapgpu_sssp_labels_noalloc(NOALLOC_MAX_NODES1 + 1, *args)
+    assert rc == _capi.TAPGPU_ERR_UNSUPPORTED
+    assert lib.tapgpu_sssp_labels_noalloc(NOALLOC_MAX_NODES1, *args) == _capi.TAPGPU_OK

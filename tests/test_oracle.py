@@ -103,7 +103,8 @@ def test_oracle_matches_live_reference(threads):
 def test_oracle_sssp_chicago_regional():
     """The reference's own ChicagoRegional graph (12,982 nodes): labels and
     predecessors of the port equal sssp_pape_lll's for a sample of sources."""
-    path = "/root/reference/trunk/cuda_sssp_double/rmat.txt.chicagoregionalflows"
+    from oracle import build_oracle as ob
+    path = os.path.join(ob.REF_TRUNK, "cuda_sssp_double", "rmat.txt.chicagoregionalflows")
     if not os.path.exists(path):
         pytest.skip("graph file absent")
     with open(path) as f:

@@ -8,6 +8,10 @@
 // weights, the sources and the output in device memory, and the only other
 // memory used is the fixed array below, which every GPU that loads the
 // library holds until the process exits.
+//
+// One call = one memset of the control block, one input check kernel, one
+// shortest-path launch and one 4-byte status read-back: the caller's stream
+// is synchronised once, at the end.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -18,53 +22,65 @@
 
 namespace {
 
-// 32 MiB: a 256-byte control block (work counter, error word) followed by
-// per-CTA label slices of (8 (N+1) + bitmap) bytes each.
+// 32 MiB: a 256-byte control block (work counter, error word, missing-path
+// info) followed by per-CTA label slices of (8 (N+1) + bitmap) bytes each.
 constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;
 constexpr size_t kControlBytes = 256;
-constexpr int kMaxDevices = 64;
 constexpr int kBlock = 256;
+constexpr int kCheckBlock = 256;
+// error bit of the input check (the path kernels' own bits are below it)
+constexpr int kErrBadInput = 1 << 20;
+// a work counter this high makes every CTA of the persistent path kernel
+// find no task, so it leaves the caller's buffers untouched
+constexpr int kNoTasks = 1 << 30;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-// Device address of g_noalloc_scratch per device; looked up once per device
-// (with that device current), because in host code the symbol's name only
-// stands for the array and is not a device address.
-void* g_scratch_addr[kMaxDevices] = {nullptr};
-
-int scratch_address(int dev, unsigned char** out) {
-  if (dev < 0 || dev >= kMaxDevices) return TAPGPU_ERR_UNSUPPORTED;
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
-      cudaGetLastError();
-      return TAPGPU_ERR_CUDA;
-    }
-    g_scratch_addr[dev] = p;
+// The array's device address, looked up on every call with the caller's
+// device current: in host code the symbol's name stands for the array and is
+// not a device address, and a lookup per call stays valid after a device
+// reset or under another context.
+int scratch_address(unsigned char** out) {
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p) {
+    cudaGetLastError();
+    return TAPGPU_ERR_CUDA;
   }
-  *out = static_cast<unsigned char*>(g_scratch_addr[dev]);
+  *out = static_cast<unsigned char*>(p);
   return TAPGPU_OK;
 }
 
-// Check device-resident indices through a fixed stack buffer (no allocation):
-// every value in [lo, hi], and non-decreasing when `monotone`.
-int check_indices(const int32_t* d, int64_t n, int32_t lo, int32_t hi, bool monotone,
-                  cudaStream_t s) {
-  int32_t buf[1024];
-  int32_t prev = lo;
-  for (int64_t i0 = 0; i0 < n; i0 += 1024) {
-    const int64_t cnt = n - i0 < 1024 ? n - i0 : 1024;
-    if (cudaMemcpyAsync(buf, d + i0, sizeof(int32_t) * cnt, cudaMemcpyDeviceToHost, s) !=
-            cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess)
-      return TAPGPU_ERR_CUDA;
-    for (int64_t i = 0; i < cnt; ++i) {
-      if (buf[i] < lo || buf[i] > hi || (monotone && buf[i] < prev)) return TAPGPU_ERR_ARG;
-      prev = buf[i];
+// Checks the caller's device-resident indices and weights before the path
+// kernel reads them: row_ptr non-decreasing within 0..num_links,
+// heads and sources in 0..num_nodes1-1, weights >= 0 (NaN fails).  On a
+// failure it sets kErrBadInput and moves the work counter past every task.
+__global__ void __launch_bounds__(kCheckBlock)
+    k_check_inputs(int n1, int m, const int32_t* row_ptr, const int32_t* head, const double* w,
+                   const int32_t* sources, int num_sources, int* counter, int* err) {
+  const int64_t n = static_cast<int64_t>(n1) + 1;
+  int64_t longest = n > m ? n : m;
+  if (num_sources > longest) longest = num_sources;
+  bool bad = false;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * kCheckBlock + threadIdx.x; i < longest;
+       i += static_cast<int64_t>(gridDim.x) * kCheckBlock) {
+    if (i < n) {
+      const int32_t r = row_ptr[i];
+      bad |= r < 0 || r > m || (i + 1 < n && row_ptr[i + 1] < r);
+    }
+    if (i < m) {
+      const int32_t h = head[i];
+      bad |= h < 0 || h >= n1 || !(w[i] >= 0.0);
+    }
+    if (i < num_sources) {
+      const int32_t s = sources[i];
+      bad |= s < 0 || s >= n1;
     }
   }
-  return TAPGPU_OK;
+  if (__syncthreads_or(bad) && threadIdx.x == 0) {
+    atomicOr(err, kErrBadInput);
+    atomicExch(counter, kNoTasks);
+  }
 }
 
 }  // namespace
@@ -79,7 +95,7 @@ extern "C" int tapgpu_sssp_labels_noalloc(int32_t num_nodes1, int32_t num_links,
     fprintf(stderr, "tapgpu_sssp_labels_noalloc: invalid argument\n");
     return TAPGPU_ERR_ARG;
   }
-  if (num_sources == 0) return TAPGPU_OK;
+  // the size limit comes first, before any CUDA call
   const size_t slice = tapgpu::sssp_smem_bytes(num_nodes1, true);
   const size_t room = kNoAllocScratchBytes - kControlBytes;
   if (slice > room) {
@@ -89,10 +105,11 @@ extern "C" int tapgpu_sssp_labels_noalloc(int32_t num_nodes1, int32_t num_links,
             num_nodes1, slice, room);
     return TAPGPU_ERR_UNSUPPORTED;
   }
+  if (num_sources == 0) return TAPGPU_OK;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return TAPGPU_ERR_NO_DEVICE;
   unsigned char* base = nullptr;
-  int rc = scratch_address(dev, &base);
+  int rc = scratch_address(&base);
   if (rc != TAPGPU_OK) {
     fprintf(stderr, "tapgpu_sssp_labels_noalloc: cudaGetSymbolAddress failed\n");
     return rc;
@@ -110,17 +127,20 @@ extern "C" int tapgpu_sssp_labels_noalloc(int32_t num_nodes1, int32_t num_links,
   int* err = counter + 1;
   int* err_info = counter + 2;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  // indices come from the caller's device memory: check them before any kernel uses them
-  if (check_indices(d_row_ptr, int64_t(num_nodes1) + 1, 0, num_links, true, s) != TAPGPU_OK ||
-      check_indices(d_head, num_links, 0, num_nodes1 - 1, false, s) != TAPGPU_OK ||
-      check_indices(d_sources, num_sources, 0, num_nodes1 - 1, false, s) != TAPGPU_OK) {
-    fprintf(stderr,
-            "tapgpu_sssp_labels_noalloc: forward star or sources out of range "
-            "(row_ptr must run 0..num_links, heads and sources 0..num_nodes1-1)\n");
-    return TAPGPU_ERR_ARG;
-  }
   // the array keeps the previous call's contents: clear the control block
   if (cudaMemsetAsync(base, 0, kControlBytes, s) != cudaSuccess) return TAPGPU_ERR_CUDA;
+  // indices come from the caller's device memory: checked on the device
+  // before the path kernel uses them (a failed check leaves it no task)
+  {
+    int64_t longest = static_cast<int64_t>(num_nodes1) + 1;
+    if (num_links > longest) longest = num_links;
+    if (num_sources > longest) longest = num_sources;
+    int64_t cgrid = (longest + kCheckBlock - 1) / kCheckBlock;
+    if (cgrid > 4 * static_cast<int64_t>(sms)) cgrid = 4 * static_cast<int64_t>(sms);
+    k_check_inputs<<<static_cast<int>(cgrid), kCheckBlock, 0, s>>>(
+        num_nodes1, num_links, d_row_ptr, d_head, d_weight, d_sources, num_sources, counter, err);
+    if (cudaGetLastError() != cudaSuccess) return TAPGPU_ERR_CUDA;
+  }
 
   tapgpu::PathArgs a{};
   a.g.n1 = num_nodes1;
@@ -148,5 +168,12 @@ extern "C" int tapgpu_sssp_labels_noalloc(int32_t num_nodes1, int32_t num_links,
   if (cudaMemcpyAsync(&e, err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess)
     return TAPGPU_ERR_CUDA;
+  if (e & kErrBadInput) {
+    fprintf(stderr,
+            "tapgpu_sssp_labels_noalloc: forward star, weights or sources out of range "
+            "(row_ptr must be non-decreasing within 0..num_links, heads and sources lie in "
+            "0..num_nodes1-1, weights >= 0)\n");
+    return TAPGPU_ERR_ARG;
+  }
   return e ? TAPGPU_ERR_NO_CONVERGENCE : TAPGPU_OK;
 }

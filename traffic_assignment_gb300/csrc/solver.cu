@@ -1019,6 +1019,16 @@ int tapgpu_solve_scenarios(tapgpu_ctx* ctx, int num_scen, const int64_t* scen_pt
   }
   Ctx* c = ctx->c;
   const int M = c->M;
+  // every argument is checked before the context's state changes
+  const int64_t nedit = scen_ptr[num_scen] - scen_ptr[0];
+  if (nedit > std::numeric_limits<int>::max() - 1) {
+    tapgpu::set_message("too many scenario edits in one call");
+    return TAPGPU_ERR_ARG;
+  }
+  if (nedit > 0 && (!scen_links || !scen_cap)) {
+    tapgpu::set_message("scenario edits without link or capacity arrays");
+    return TAPGPU_ERR_ARG;
+  }
   std::vector<int64_t> inv(M);
   for (int k = 0; k < M; ++k) inv[c->perm[k]] = k;
   for (int s = 0; s < num_scen; ++s) {
@@ -1049,11 +1059,6 @@ int tapgpu_solve_scenarios(tapgpu_ctx* ctx, int num_scen, const int64_t* scen_pt
     std::stable_sort(c->h_cap_order.begin(), c->h_cap_order.end(),
                      [c](int a, int b) { return c->h_cap[a] < c->h_cap[b]; });
     c->base_dirty = false;
-  }
-  const int64_t nedit = scen_ptr[num_scen] - scen_ptr[0];
-  if (nedit > std::numeric_limits<int>::max() - 1) {
-    tapgpu::set_message("too many scenario edits in one call");
-    return TAPGPU_ERR_ARG;
   }
   std::vector<int> eptr(num_scen + 1), elink(static_cast<size_t>(std::max<int64_t>(nedit, 1)));
   std::vector<double> evalv(elink.size()), emin(num_scen);
