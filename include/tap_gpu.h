@@ -357,6 +357,26 @@ int tapgpu_get_tape(tapgpu_ctx *ctx, int scenario, int iteration, double *x_chec
  * solves (tapgpu_solve) always use the base demand. */
 int tapgpu_set_scenario_demand(tapgpu_ctx *ctx, int num_scen, const double *demand);
 
+/* Link-record scenarios: the batched form of the ADD and CHANGE records of a
+ * net-mods file, which the reference's scenario farm applies to one network
+ * copy per scenario before solving it alone (tap/tap_mpi_main.c:201-240,
+ * 678-753).  The context's network is the union of every scenario's links
+ * (the base links and each added link once).  From the next
+ * tapgpu_solve_scenarios call with num_scen scenarios on, scenario s uses
+ * free-flow time edit_fft[i], BPR alpha edit_alpha[i] and power
+ * edit_beta[i] on link edit_links[i] for i in edit_ptr[s] .. edit_ptr[s+1]-1
+ * (the base values elsewhere; capacities come from that call's capacity
+ * edits), and does not have links absent_links[absent_ptr[s] ..
+ * absent_ptr[s+1]-1] at all: they carry no flow, are never on a path and are
+ * left out of its zero-capacity fix-up.  A warm start gives added links zero
+ * flow, as tap/tap_frankwolfe_pthread.c:564-597 inserts them.  num_scen 0
+ * returns to the one base network; single solves (tapgpu_solve) always use
+ * it. */
+int tapgpu_set_scenario_links(tapgpu_ctx *ctx, int num_scen, const int64_t *edit_ptr,
+                              const int64_t *edit_links, const double *edit_fft,
+                              const double *edit_alpha, const double *edit_beta,
+                              const int64_t *absent_ptr, const int64_t *absent_links);
+
 /* Shortest-path work counters gathered while timing is on (out has 6
  * entries): out[0] label correction rounds or near-far phases, out[1]
  * (scenario, origin) tasks, out[2] node expansions, and for the near-far

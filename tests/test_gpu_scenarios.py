@@ -6,6 +6,7 @@ import numpy as np
 import pytest
 
 import oracle
+from mods_fixtures import mixed_mods
 from traffic_assignment_gb300 import Solver, scenarios, synth, tntp
 
 pytestmark = pytest.mark.gpu
@@ -228,3 +229,59 @@ def test_demand_scenario_matches_reference_trip_mods_golden(built_lib):
     assert _rel(x, z["volume"]) < 1e-6
     assert _rel(t, z["cost"]) < 1e-6
     assert abs(res[0]["total_cost"] - float(z["hdr_totalcost"])) <= 1e-6 * float(z["hdr_totalcost"])
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-6), ("fp32", 1e-4)])
+def test_link_record_scenarios_match_oracle(built_lib, precision, tol):
+    """Net-mods records of every kind (capacity and free-flow-time CHANGEs,
+    ADDs, an ADD changed by a later record, a zero capacity) as one batch over
+    the union network, warm-started from the base flows with zero flow on the
+    added links (tap/tap_frankwolfe_pthread.c:564-597): each scenario against
+    the oracle solving that scenario's own network (tap/tap_mpi_main.c:201-240
+    applied, links sorted) from the same warm start.  FP64: flows, VHT and
+    relative gap within 1e-6 and the same step every iteration; FP32 paths:
+    flows within 1e-4."""
+    net, dem = synth.make_grid416()
+    groups = scenarios.group_mods(mixed_mods(net))
+    scen = scenarios.enumerate_scenarios(list(groups), "pairs")
+    recs = [(sid, [m for c in sel for m in groups[c]]) for sid, sel in scen]
+    b = scenarios.build_link_batch(net, recs)
+    base = oracle.frankwolfe(net, dem, threads=1, max_iters=40)
+    x0 = b.warm_start(base["x"])
+    K = 30
+    with Solver(b.union, dem, precision=precision) as s:
+        s.set_scenario_links(b.edits, b.absent)
+        res = s.solve_scenarios(b.scenarios, max_iters=K, x0=x0)
+        flows = [s.flows(i)[0] for i in range(len(recs))]
+        traces = [s.trace(i, max_rows=100) for i in range(len(recs))]
+    for i, (sid, _) in enumerate(recs):
+        order = b.scenario_order(i)
+        assert np.all(flows[i][b.absent[i]] == 0.0), sid
+        ref = oracle.frankwolfe(b.scenario_network(i), dem, threads=1, max_iters=K,
+                                x0=x0[order])
+        assert res[i]["error_bits"] == 0 and res[i]["iterations"] == K
+        assert _rel(flows[i][order], ref["x"]) < tol, sid
+        if precision == "fp64":
+            assert abs(res[i]["total_cost"] - ref["total_cost"]) <= tol * ref["total_cost"], sid
+            assert abs(res[i]["relgap"] - ref["relgap"]) <= tol * abs(ref["relgap"]), sid
+            np.testing.assert_array_equal(traces[i][:, 4], ref["trace"][:, 4], err_msg=sid)
+
+
+def test_farm_batches_link_records(built_lib, tmp_path):
+    """solve_farm solves ADD / CHANGE scenarios in one batch (no per-scenario
+    contexts): the same VHT as the union-network batch solved directly."""
+    net, dem = synth.make_grid416()
+    mods = mixed_mods(net)
+    path = str(tmp_path / "mods.txt")
+    with open(path, "w") as f:
+        for m in mods:
+            f.write("\t".join([m.change_id, m.kind] + [repr(v) if isinstance(v, float) else str(v)
+                                                        for v in m.link] + ["0"]) + "\n")
+    out = scenarios.solve_farm(net, dem, path, "single", target_relgap=0, max_iters=12,
+                               warm_start=False, precision="fp64")
+    assert [d["id"] for d in out] == list(scenarios.group_mods(mods))
+    assert all(d["batched"] for d in out)
+    for d, sid in zip(out, scenarios.group_mods(mods)):
+        recs = scenarios.group_mods(mods)[sid]
+        ref = oracle.frankwolfe(scenarios.apply_mods(net, recs), dem, threads=1, max_iters=12)
+        assert abs(d["total_cost"] - ref["total_cost"]) <= 1e-6 * ref["total_cost"], sid

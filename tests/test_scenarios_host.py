@@ -3,6 +3,7 @@
 import numpy as np
 import pytest
 
+from mods_fixtures import mixed_mods
 from traffic_assignment_gb300 import scenarios, synth
 
 
@@ -37,3 +38,28 @@ def test_apply_mods_change_and_add():
     assert np.all(np.diff(n2.init * 100 + n2.term) >= 0)
     grouped = scenarios.group_mods([add, ch])
     assert list(grouped) == ["u1", "u2"]
+
+
+@pytest.mark.parametrize("mode", ["single", "pairs", "subsets"])
+def test_link_batch_reproduces_each_scenario_network(mode):
+    """The union network with each scenario's capacity and parameter edits,
+    restricted to its own links, is the network the reference's farm builds
+    for that scenario (tap/tap_mpi_main.c:201-240 records, then sorted)."""
+    net, _ = synth.make_grid416()
+    mods = mixed_mods(net)
+    groups = scenarios.group_mods(mods)
+    scen = scenarios.enumerate_scenarios(list(groups), mode)
+    recs = [(sid, [m for c in sel for m in groups[c]]) for sid, sel in scen]
+    b = scenarios.build_link_batch(net, recs)
+    assert b.union.num_links == net.num_links + 3  # each ADD record once
+    for s, (sid, r) in enumerate(recs):
+        want = scenarios.apply_mods(net, r)
+        got = b.scenario_network(s)
+        for f in ("init", "term", "capacity", "fft", "alpha", "beta"):
+            np.testing.assert_array_equal(getattr(got, f), getattr(want, f), err_msg=f"{sid} {f}")
+        # links of the union that the scenario lacks are exactly the others' additions
+        mine = set(b.members[s].tolist())
+        assert set(b.absent[s].tolist()) == set(range(net.num_links, b.union.num_links)) - mine
+    assert b.needs_links
+    x = b.warm_start(np.arange(net.num_links, dtype=float))
+    assert np.all(x[net.num_links:] == 0) and x[7] == 7

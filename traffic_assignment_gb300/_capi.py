@@ -82,6 +82,7 @@ EXPORTED = [
     "tapgpu_profile_iteration", "tapgpu_run_iterations", "tapgpu_set_timing",
     "tapgpu_get_timing", "tapgpu_get_path_stats", "tapgpu_sssp_labels_noalloc",
     "tapgpu_adjoint_vht", "tapgpu_get_tape", "tapgpu_set_scenario_demand",
+    "tapgpu_set_scenario_links",
 ]
 EXPORTED_DATA = ["num_cores", "num_threads", "using_fermi_architecture"]
 
@@ -140,6 +141,9 @@ def load(path: str | None = None):
     L.tapgpu_get_tape.restype = C.c_int
     L.tapgpu_set_scenario_demand.argtypes = [vp, C.c_int, F64P]
     L.tapgpu_set_scenario_demand.restype = C.c_int
+    L.tapgpu_set_scenario_links.argtypes = [vp, C.c_int, I64P, I64P, F64P, F64P, F64P, I64P,
+                                            I64P]
+    L.tapgpu_set_scenario_links.restype = C.c_int
     for fn in ("tapgpu_create", "tapgpu_solve", "tapgpu_solve_begin", "tapgpu_solve_advance",
                "tapgpu_get_link_flows", "tapgpu_get_link_flows_batch", "tapgpu_get_trace",
                "tapgpu_set_capacity", "tapgpu_solve_scenarios", "tapgpu_sssp", "tapgpu_aon",

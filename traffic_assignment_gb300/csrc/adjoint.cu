@@ -187,7 +187,7 @@ int tapgpu_adjoint_vht(tapgpu_ctx* ctx, int scenario, double* grad, double* vht)
   const size_t off = static_cast<size_t>(scenario) * M;
   const size_t nck = static_cast<size_t>(c->hist_cap / C + 1);
   cudaStream_t s = c->stream;
-  tapgpu::k_adj_init<<<grid, tapgpu::kAdjBlock, 0, s>>>(M, c->link_params(), c->cap + off,
+  tapgpu::k_adj_init<<<grid, tapgpu::kAdjBlock, 0, s>>>(M, c->link_params_of(scenario), c->cap + off,
                                                          c->x + off, c->adj_xbar, c->adj_cbar);
   TA_CUDA(cudaGetLastError());
   const double* dh = c->d_hist + static_cast<size_t>(scenario) * c->hist_cap * M;
@@ -202,7 +202,7 @@ int tapgpu_adjoint_vht(tapgpu_ctx* ctx, int scenario, double* grad, double* vht)
     for (int k = k0 + len - 1; k >= k0; --k) {
       tapgpu::AdjArgs a;
       a.m = M;
-      a.lp = c->link_params();
+      a.lp = c->link_params_of(scenario);
       a.cap = c->cap + off;
       a.x = c->adj_seg + static_cast<size_t>(k - k0) * M;
       a.d = dh + static_cast<size_t>(k) * M;

@@ -1557,8 +1557,22 @@ __device__ __forceinline__ bool last_block(unsigned* arrive) {
   return sh_ticket == gridDim.x - 1;
 }
 
-// shortest-path weight of link k of scenario scen in every record layout
+// index of link k's parameters for scenario scen (shared row or per-scenario rows)
+__device__ __forceinline__ size_t lpi(const LinkParams& lp, int scen, int k) {
+  return static_cast<size_t>(scen) * static_cast<size_t>(lp.stride) + static_cast<size_t>(k);
+}
+
+// link k is not part of scenario scen's network (a link another scenario adds)
+__device__ __forceinline__ bool is_absent(const LinkArgs& a, int scen, int k) {
+  return a.absent &&
+         ((__ldg(a.absent + static_cast<size_t>(scen) * a.absent_words + (k >> 5)) >> (k & 31)) & 1u);
+}
+
+// shortest-path weight of link k of scenario scen in every record layout; a
+// link absent from the scenario's network gets +inf, so it never relaxes a
+// label and never enters a predecessor tree
 __device__ __forceinline__ void write_weights(const LinkArgs& a, int scen, int k, double t) {
+  if (is_absent(a, scen, k)) t = __longlong_as_double(0x7ff0000000000000ll);
   const size_t i = static_cast<size_t>(scen) * a.m + k;
   if (a.e32) {
     const unsigned bits = __float_as_uint(__double2float_rn(t));
@@ -1585,15 +1599,21 @@ __global__ void __launch_bounds__(kLinkBlock) k_init_flows(LinkArgs a, int from_
     double x;
     if (from_x) {
       x = a.x[off + k];
+      if (is_absent(a, scen, k) && x != 0.0) {  // a link the scenario does not have carries nothing
+        x = 0.0;
+        a.x[off + k] = x;
+      }
     } else {
       x = static_cast<double>(static_cast<long long>(a.y_fx[off + k])) * a.inv_scale;
       a.x[off + k] = x;
     }
     a.y_fx[off + k] = 0ull;
-    const double t = bpr(a.lp.fft[k], a.lp.alpha[k], a.lp.beta[k], a.lp.ipow[k], cap[k], x);
+    const size_t pk = lpi(a.lp, scen, k);
+    const double t = bpr(a.lp.fft[pk], a.lp.alpha[pk], a.lp.beta[pk], a.lp.ipow[pk], cap[k], x);
     a.t[off + k] = t;
     if (a.dtdx)
-      a.dtdx[off + k] = bpr_dq(a.lp.fft[k], a.lp.alpha[k], a.lp.beta[k], a.lp.ipow[k], cap[k], x);
+      a.dtdx[off + k] =
+          bpr_dq(a.lp.fft[pk], a.lp.alpha[pk], a.lp.beta[pk], a.lp.ipow[pk], cap[k], x);
     write_weights(a, scen, k, t);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -1620,7 +1640,7 @@ __global__ void __launch_bounds__(kLinkBlock) k_set_free_flow(LinkArgs a) {
   const size_t off = static_cast<size_t>(scen) * a.m;
   for (int k = blockIdx.x * kLinkBlock + threadIdx.x; k < a.m; k += gridDim.x * kLinkBlock) {
     a.y_fx[off + k] = 0ull;
-    write_weights(a, scen, k, a.lp.fft[k]);
+    write_weights(a, scen, k, a.lp.fft[lpi(a.lp, scen, k)]);
   }
 }
 
@@ -1707,8 +1727,9 @@ __global__ void __launch_bounds__(kLinkBlock) k_ls_pass(LinkArgs a) {
   const double* cap = a.cap + off;
   for (int k = blockIdx.x * kLinkBlock + threadIdx.x; k < a.m; k += gridDim.x * kLinkBlock) {
     const double x = a.x[off + k];
-    const double fft = a.lp.fft[k], al = a.lp.alpha[k], be = a.lp.beta[k], c = cap[k];
-    const unsigned char ip = a.lp.ipow[k];
+    const size_t pk = lpi(a.lp, scen, k);
+    const double fft = a.lp.fft[pk], al = a.lp.alpha[pk], be = a.lp.beta[pk], c = cap[k];
+    const unsigned char ip = a.lp.ipow[pk];
     // FP32-path mode, integer power: t(x + lam d) = fft + (fft alpha) (x/c + lam d/c)^beta
     // with one division per link (FP64 mode keeps the reference's forms,
     // tap/tap_functions.c:55-65, 112-126)
@@ -1796,7 +1817,8 @@ __global__ void __launch_bounds__(1024) k_ls_fallback(LinkArgs a) {
     for (int k = threadIdx.x; k < a.m; k += blockDim.x) {
       const double x = a.x[off + k], d = a.d[off + k];
       const double q = __dadd_rn(x, __dmul_rn(lam, d));
-      s = __dadd_rn(s, __dmul_rn(bpr(a.lp.fft[k], a.lp.alpha[k], a.lp.beta[k], a.lp.ipow[k],
+      const size_t pk = lpi(a.lp, scen, k);
+      s = __dadd_rn(s, __dmul_rn(bpr(a.lp.fft[pk], a.lp.alpha[pk], a.lp.beta[pk], a.lp.ipow[pk],
                                      cap[k], q), d));
     }
     for (int o = 16; o >= 1; o >>= 1) s += __shfl_down_sync(kFull, s, o);
@@ -1845,8 +1867,9 @@ __global__ void __launch_bounds__(kLinkBlock) k_step(LinkArgs a) {
     if (ckpt) a.x_hist[xoff + k] = x0;
     const double x = __dadd_rn(x0, __dmul_rn(lam, d));
     a.x[off + k] = x;
-    const double fft = a.lp.fft[k], al = a.lp.alpha[k], be = a.lp.beta[k], c = cap[k];
-    const unsigned char ip = a.lp.ipow[k];
+    const size_t pk = lpi(a.lp, scen, k);
+    const double fft = a.lp.fft[pk], al = a.lp.alpha[pk], be = a.lp.beta[pk], c = cap[k];
+    const unsigned char ip = a.lp.ipow[pk];
     const double t = bpr(fft, al, be, ip, c, x);
     a.t[off + k] = t;
     if (a.dtdx) a.dtdx[off + k] = bpr_dq(fft, al, be, ip, c, x);
@@ -2124,6 +2147,43 @@ cudaError_t launch_scenario_caps(double* cap, const double* base, int m, int nsc
   k_scen_edits<<<(nscen + kLinkBlock - 1) / kLinkBlock, kLinkBlock, 0, s>>>(cap, m, nscen, ptr, link,
                                                                            val, min_pos);
   return cudaGetLastError();
+}
+
+// per-scenario link parameter rows: base row everywhere, then each scenario's edits
+template <typename T>
+__global__ void __launch_bounds__(kLinkBlock) k_rows_of_base(T* rows, const T* base, int m) {
+  const size_t row = static_cast<size_t>(blockIdx.y) * m;
+  for (int k = blockIdx.x * kLinkBlock + threadIdx.x; k < m; k += gridDim.x * kLinkBlock)
+    rows[row + k] = base[k];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kLinkBlock) k_row_edits(T* rows, int m, int nscen, const int* ptr,
+                                                          const int* link, const T* val) {
+  const int s = blockIdx.x * kLinkBlock + threadIdx.x;
+  if (s >= nscen) return;
+  T* row = rows + static_cast<size_t>(s) * m;
+  for (int i = ptr[s]; i < ptr[s + 1]; ++i) row[link[i]] = val[i];
+}
+
+template <typename T>
+cudaError_t launch_param_rows_t(T* rows, const T* base, int m, int nscen, const int* ptr,
+                                const int* link, const T* val, int grid, cudaStream_t s) {
+  k_rows_of_base<T><<<dim3(grid, nscen), kLinkBlock, 0, s>>>(rows, base, m);
+  k_row_edits<T><<<(nscen + kLinkBlock - 1) / kLinkBlock, kLinkBlock, 0, s>>>(rows, m, nscen, ptr,
+                                                                             link, val);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_param_rows(double* rows, const double* base, int m, int nscen, const int* ptr,
+                              const int* link, const double* val, int grid, cudaStream_t s) {
+  return launch_param_rows_t(rows, base, m, nscen, ptr, link, val, grid, s);
+}
+
+cudaError_t launch_param_rows(unsigned char* rows, const unsigned char* base, int m, int nscen,
+                              const int* ptr, const int* link, const unsigned char* val, int grid,
+                              cudaStream_t s) {
+  return launch_param_rows_t(rows, base, m, nscen, ptr, link, val, grid, s);
 }
 
 cudaError_t launch_replicate_rows(double* x, int m, int nscen, int grid, cudaStream_t s) {

@@ -46,6 +46,7 @@ struct LinkParams {
   const double* alpha;
   const double* beta;
   const unsigned char* ipow;  // 0..15: integer power; 255: use pow()
+  long long stride;           // 0: one row for every scenario; m: row [scenario][m]
 };
 
 struct ScenState {
@@ -145,6 +146,8 @@ struct LinkArgs {
   int ckpt_every;               // flows kept every ckpt_every iterations
   int ls_mode;                  // kLsReference or kLsExact
   int ls_ratio;                 // FP32-path mode: candidates from x/c + lambda d/c (one division)
+  const unsigned* absent;       // [S][absent_words] links not in a scenario's network, or null
+  int absent_words;             // 32-bit words per scenario of `absent`
 };
 
 // launch helpers (implemented in fw_kernels.cu)
@@ -176,6 +179,12 @@ cudaError_t launch_step(const LinkArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_scenario_caps(double* cap, const double* base, int m, int nscen, const int* ptr,
                                  const int* link, const double* val, const double* min_pos,
                                  int grid, cudaStream_t s);
+// parameter rows [nscen][m] = base with each scenario's edits (ptr [nscen+1], link, val)
+cudaError_t launch_param_rows(double* rows, const double* base, int m, int nscen, const int* ptr,
+                              const int* link, const double* val, int grid, cudaStream_t s);
+cudaError_t launch_param_rows(unsigned char* rows, const unsigned char* base, int m, int nscen,
+                              const int* ptr, const int* link, const unsigned char* val, int grid,
+                              cudaStream_t s);
 // rows 1 .. nscen-1 of x [nscen][m] become copies of row 0
 cudaError_t launch_replicate_rows(double* x, int m, int nscen, int grid, cudaStream_t s);
 int sssp_occupancy(bool fp64, int block, bool smem, int n1, int variant);  // CTAs per SM

@@ -128,10 +128,30 @@ Graph Ctx::graph() const {
 
 LinkParams Ctx::link_params() const {
   LinkParams lp;
+  if (use_link_scen && sc_fft) {
+    lp.fft = sc_fft;
+    lp.alpha = sc_alpha;
+    lp.beta = sc_beta;
+    lp.ipow = sc_ipow;
+    lp.stride = M;
+    return lp;
+  }
   lp.fft = fft;
   lp.alpha = alpha;
   lp.beta = beta;
   lp.ipow = ipow;
+  lp.stride = 0;
+  return lp;
+}
+
+LinkParams Ctx::link_params_of(int scen) const {
+  LinkParams lp = link_params();
+  const size_t off = static_cast<size_t>(scen) * static_cast<size_t>(lp.stride);
+  lp.fft += off;
+  lp.alpha += off;
+  lp.beta += off;
+  lp.ipow += off;
+  lp.stride = 0;
   return lp;
 }
 
@@ -214,6 +234,8 @@ LinkArgs Ctx::link_args(int nscen) const {
   a.ckpt_every = ckpt_every;
   a.ls_mode = ls_mode;
   a.ls_ratio = fp64 ? 0 : 1;
+  a.absent = use_link_scen ? sc_absent : nullptr;
+  a.absent_words = absent_words;
   return a;
 }
 
@@ -433,7 +455,8 @@ int Ctx::run_graph(int iters, int nscen) {
     }
     return TAPGPU_OK;
   }
-  if (!gexec || g_iters != iters || g_nscen != nscen || g_dem != use_dem_scen) {
+  if (!gexec || g_iters != iters || g_nscen != nscen || g_dem != use_dem_scen ||
+      g_links != use_link_scen) {
     if (gexec) {
       cudaGraphExecDestroy(gexec);
       gexec = nullptr;
@@ -464,6 +487,7 @@ int Ctx::run_graph(int iters, int nscen) {
     g_iters = iters;
     g_nscen = nscen;
     g_dem = use_dem_scen;
+    g_links = use_link_scen;
   }
   TG_CUDA(cudaGraphLaunch(gexec, stream));
   launches += g_kernels;
@@ -892,6 +916,7 @@ int tapgpu_solve_begin(tapgpu_ctx* ctx, int max_iters, double target_relgap, con
   TG_CUDA(cudaSetDevice(c->device));
   TG_TRY(c->ensure_scenarios(1));
   c->use_dem_scen = false;
+  c->use_link_scen = false;
   TG_CUDA(cudaMemcpy(c->cap, c->h_cap.data(), sizeof(double) * c->M, cudaMemcpyHostToDevice));
   std::vector<int> one{0};
   TG_CUDA(cudaMemcpyAsync(c->scen_list, one.data(), sizeof(int), cudaMemcpyHostToDevice, c->stream));
@@ -1044,9 +1069,15 @@ int tapgpu_solve_scenarios(tapgpu_ctx* ctx, int num_scen, const int64_t* scen_pt
                         " scenarios, not " + std::to_string(num_scen));
     return TAPGPU_ERR_ARG;
   }
+  if (c->link_scen && c->link_scen != num_scen) {
+    tapgpu::set_message("link-record scenarios were set for " + std::to_string(c->link_scen) +
+                        " scenarios, not " + std::to_string(num_scen));
+    return TAPGPU_ERR_ARG;
+  }
   TG_CUDA(cudaSetDevice(c->device));
   TG_TRY(c->ensure_scenarios(num_scen));
   c->use_dem_scen = c->dem_scen == num_scen;
+  c->use_link_scen = c->link_scen == num_scen;
   c->last_nscen = num_scen;
   // capacities of every scenario, made on the device from the base row and
   // the edits; the host finds each scenario's smallest positive capacity
@@ -1083,6 +1114,7 @@ int tapgpu_solve_scenarios(tapgpu_ctx* ctx, int num_scen, const int64_t* scen_pt
       }
       for (int k : c->h_cap_order) {
         if (std::find(seen.begin(), seen.end(), k) != seen.end()) continue;
+        if (c->absent_in(s, k)) continue;  // not part of this scenario's network
         if (c->h_cap[k] < mn) mn = c->h_cap[k];
         break;
       }
@@ -1134,8 +1166,8 @@ int tapgpu_solve_scenarios(tapgpu_ctx* ctx, int num_scen, const int64_t* scen_pt
     TG_CUDA(tapgpu::launch_replicate_rows(c->x, M, num_scen, c->link_grid, c->stream));
     TG_CUDA(cudaStreamSynchronize(c->stream));
     TG_TRY(c->enqueue_initial(num_scen, true));
-  } else if (c->use_dem_scen) {
-    // every scenario has its own demand: load each at free flow
+  } else if (c->use_dem_scen || c->use_link_scen) {
+    // every scenario has its own demand or links: load each at its own free flow
     tapgpu::LinkArgs la = c->link_args(num_scen);
     TG_CUDA(tapgpu::launch_set_costs(la, c->link_grid, c->stream));
     TG_TRY(c->enqueue_paths(num_scen, true, c->e32, c->r32, c->w64, c->yfx, true));
@@ -1227,6 +1259,135 @@ int tapgpu_set_scenario_demand(tapgpu_ctx* ctx, int num_scen, const double* dema
   TG_CUDA(cudaMemcpy(c->sc_od_q, q.data(), sizeof(long long) * q.size(), cudaMemcpyHostToDevice));
   TG_CUDA(cudaMemcpy(c->sc_total, totals.data(), sizeof(double) * num_scen, cudaMemcpyHostToDevice));
   c->dem_scen = num_scen;
+  return TAPGPU_OK;
+}
+
+int tapgpu_set_scenario_links(tapgpu_ctx* ctx, int num_scen, const int64_t* edit_ptr,
+                              const int64_t* edit_links, const double* edit_fft,
+                              const double* edit_alpha, const double* edit_beta,
+                              const int64_t* absent_ptr, const int64_t* absent_links) {
+  if (!ctx || num_scen < 0) return TAPGPU_ERR_ARG;
+  Ctx* c = ctx->c;
+  const int M = c->M;
+  if (num_scen > 0) {  // every argument is checked before the context's state changes
+    if (!edit_ptr || !absent_ptr) {
+      tapgpu::set_message("link-record scenarios need edit and absent-link offsets");
+      return TAPGPU_ERR_ARG;
+    }
+    const int64_t ne = edit_ptr[num_scen] - edit_ptr[0];
+    const int64_t na = absent_ptr[num_scen] - absent_ptr[0];
+    if (ne < 0 || na < 0 || ne > std::numeric_limits<int>::max() - 1 ||
+        (ne > 0 && (!edit_links || !edit_fft || !edit_alpha || !edit_beta)) ||
+        (na > 0 && !absent_links)) {
+      tapgpu::set_message("bad link-record scenario arrays");
+      return TAPGPU_ERR_ARG;
+    }
+    for (int s = 0; s < num_scen; ++s) {
+      if (edit_ptr[s + 1] < edit_ptr[s] || absent_ptr[s + 1] < absent_ptr[s]) {
+        tapgpu::set_message("link-record scenario offsets not monotone");
+        return TAPGPU_ERR_ARG;
+      }
+      for (int64_t i = edit_ptr[s]; i < edit_ptr[s + 1]; ++i) {
+        if (edit_links[i] < 0 || edit_links[i] >= M || !(edit_fft[i] >= 0) ||
+            !std::isfinite(edit_fft[i]) || !(edit_alpha[i] >= 0) ||
+            !std::isfinite(edit_alpha[i]) || !std::isfinite(edit_beta[i])) {
+          tapgpu::set_message("link-record edit " + std::to_string(i) +
+                              " has a link out of range or an invalid cost parameter");
+          return TAPGPU_ERR_ARG;
+        }
+      }
+      for (int64_t i = absent_ptr[s]; i < absent_ptr[s + 1]; ++i)
+        if (absent_links[i] < 0 || absent_links[i] >= M) {
+          tapgpu::set_message("absent link index out of range");
+          return TAPGPU_ERR_ARG;
+        }
+    }
+  }
+  TG_CUDA(cudaSetDevice(c->device));
+  TG_CUDA(cudaStreamSynchronize(c->stream));
+  void* olds[] = {c->sc_fft, c->sc_alpha, c->sc_beta, c->sc_ipow, c->sc_absent};
+  for (void* p : olds) tapgpu::free_owned(c, p);
+  c->sc_fft = c->sc_alpha = c->sc_beta = nullptr;
+  c->sc_ipow = nullptr;
+  c->sc_absent = nullptr;
+  c->h_absent.clear();
+  c->link_scen = 0;
+  c->use_link_scen = false;
+  if (c->gexec) {  // captured launches hold the old parameter pointers
+    cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+  }
+  c->g_nscen = -1;
+  if (num_scen == 0) return TAPGPU_OK;
+
+  std::vector<int64_t> inv(M);
+  for (int k = 0; k < M; ++k) inv[c->perm[k]] = k;
+  const int64_t ne = edit_ptr[num_scen] - edit_ptr[0];
+  std::vector<int> eptr(num_scen + 1), elink(static_cast<size_t>(std::max<int64_t>(ne, 1)));
+  std::vector<double> efft(elink.size()), ealpha(elink.size()), ebeta(elink.size());
+  std::vector<unsigned char> eip(elink.size());
+  int64_t j = 0;
+  for (int s = 0; s < num_scen; ++s) {
+    eptr[s] = static_cast<int>(j);
+    for (int64_t i = edit_ptr[s]; i < edit_ptr[s + 1]; ++i, ++j) {
+      elink[j] = static_cast<int>(inv[edit_links[i]]);
+      efft[j] = edit_fft[i];
+      ealpha[j] = edit_alpha[i];
+      const double b = edit_beta[i];
+      ebeta[j] = b;
+      eip[j] = (b >= 0 && b <= 15 && std::floor(b) == b) ? static_cast<unsigned char>(b) : 255;
+    }
+  }
+  eptr[num_scen] = static_cast<int>(j);
+  const int words = (M + 31) / 32;
+  c->h_absent.assign(static_cast<size_t>(num_scen) * words, 0u);
+  for (int s = 0; s < num_scen; ++s)
+    for (int64_t i = absent_ptr[s]; i < absent_ptr[s + 1]; ++i) {
+      const int k = static_cast<int>(inv[absent_links[i]]);
+      c->h_absent[static_cast<size_t>(s) * words + (k >> 5)] |= 1u << (k & 31);
+    }
+  const size_t rows = static_cast<size_t>(num_scen) * M;
+  TG_TRY(c->alloc_n(&c->sc_fft, rows));
+  TG_TRY(c->alloc_n(&c->sc_alpha, rows));
+  TG_TRY(c->alloc_n(&c->sc_beta, rows));
+  TG_TRY(c->alloc_n(&c->sc_ipow, rows));
+  TG_TRY(c->alloc_n(&c->sc_absent, c->h_absent.size()));
+  int* d_ptr = nullptr;
+  int* d_link = nullptr;
+  double* d_val = nullptr;
+  unsigned char* d_ip = nullptr;
+  TG_TRY(c->alloc_n(&d_ptr, eptr.size()));
+  TG_TRY(c->alloc_n(&d_link, elink.size()));
+  TG_TRY(c->alloc_n(&d_val, 3 * elink.size()));
+  TG_TRY(c->alloc_n(&d_ip, elink.size()));
+  const size_t ns = elink.size();
+  int rc = TAPGPU_OK;
+  if (cudaMemcpy(d_ptr, eptr.data(), sizeof(int) * eptr.size(), cudaMemcpyHostToDevice) ||
+      cudaMemcpy(d_link, elink.data(), sizeof(int) * ns, cudaMemcpyHostToDevice) ||
+      cudaMemcpy(d_val, efft.data(), sizeof(double) * ns, cudaMemcpyHostToDevice) ||
+      cudaMemcpy(d_val + ns, ealpha.data(), sizeof(double) * ns, cudaMemcpyHostToDevice) ||
+      cudaMemcpy(d_val + 2 * ns, ebeta.data(), sizeof(double) * ns, cudaMemcpyHostToDevice) ||
+      cudaMemcpy(d_ip, eip.data(), ns, cudaMemcpyHostToDevice) ||
+      cudaMemcpy(c->sc_absent, c->h_absent.data(), sizeof(unsigned) * c->h_absent.size(),
+                 cudaMemcpyHostToDevice) ||
+      tapgpu::launch_param_rows(c->sc_fft, c->fft, M, num_scen, d_ptr, d_link, d_val,
+                                c->link_grid, c->stream) ||
+      tapgpu::launch_param_rows(c->sc_alpha, c->alpha, M, num_scen, d_ptr, d_link, d_val + ns,
+                                c->link_grid, c->stream) ||
+      tapgpu::launch_param_rows(c->sc_beta, c->beta, M, num_scen, d_ptr, d_link, d_val + 2 * ns,
+                                c->link_grid, c->stream) ||
+      tapgpu::launch_param_rows(c->sc_ipow, c->ipow, M, num_scen, d_ptr, d_link, d_ip,
+                                c->link_grid, c->stream) ||
+      cudaStreamSynchronize(c->stream)) {
+    tapgpu::set_message(std::string("link-record scenario rows: ") +
+                        cudaGetErrorString(cudaGetLastError()));
+    rc = TAPGPU_ERR_CUDA;
+  }
+  void* tmp[] = {d_ptr, d_link, d_val, d_ip};
+  for (void* p : tmp) tapgpu::free_owned(c, p);
+  if (rc != TAPGPU_OK) return rc;
+  c->absent_words = words;
+  c->link_scen = num_scen;
   return TAPGPU_OK;
 }
 

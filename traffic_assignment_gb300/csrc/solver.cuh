@@ -66,6 +66,16 @@ struct Ctx {
   double* sc_total = nullptr;    // [dem_scen] demand totals
   int dem_scen = 0;              // scenarios with their own demand (0: none set)
   bool use_dem_scen = false;     // the current batched solve uses them
+  // link-record scenarios (ADD / CHANGE records): per-scenario parameter rows
+  // [link_scen][M] and a bitmask [link_scen][absent_words] of the links a
+  // scenario's network does not have
+  double *sc_fft = nullptr, *sc_alpha = nullptr, *sc_beta = nullptr;
+  unsigned char* sc_ipow = nullptr;
+  unsigned* sc_absent = nullptr;
+  std::vector<unsigned> h_absent;
+  int absent_words = 0;
+  int link_scen = 0;             // scenarios with their own link records (0: none set)
+  bool use_link_scen = false;    // the current batched solve uses them
 
   // per-scenario state (capacity for S_cap scenarios)
   int S_cap = 0;
@@ -113,7 +123,7 @@ struct Ctx {
   cudaStream_t stream = nullptr;
   cudaGraphExec_t gexec = nullptr;
   int g_iters = 0, g_nscen = -1;
-  bool g_dem = false;
+  bool g_dem = false, g_links = false;
   int solve_max_iters = 0;
   int last_nscen = 1;  // scenarios of the last solve (for run_iterations)
 
@@ -165,6 +175,12 @@ struct Ctx {
 
   Graph graph() const;
   LinkParams link_params() const;
+  // the parameters of one scenario as a single shared row
+  LinkParams link_params_of(int scen) const;
+  bool absent_in(int scen, int k) const {
+    return use_link_scen && !h_absent.empty() &&
+           ((h_absent[static_cast<size_t>(scen) * absent_words + (k >> 5)] >> (k & 31)) & 1u);
+  }
   Demand demand() const;
   PathArgs path_args(int nscen_slots) const;
   LinkArgs link_args(int nscen) const;

@@ -9,10 +9,13 @@ Modes (the farm's flags):
 
 Change ids are ordered as the farm sorts them (strncmp, :477).  A CHANGE
 record replaces the whole link record and an ADD record appends a link
-(:201-240).  Scenarios that only change capacities share topology and costs
-with the base network and are solved together by tapgpu_solve_scenarios;
-any other scenario (added links, changed free-flow time or BPR parameters) is
-solved on the GPU as its own network.
+(:201-240).  Every scenario, whatever its records, is solved in one batch
+by tapgpu_solve_scenarios: the batch's network is the union of the base
+links and each added link once (``build_link_batch``); a CHANGE becomes a
+capacity edit plus, where free-flow time or BPR parameters change, a
+per-scenario parameter edit (tapgpu_set_scenario_links); the added links of
+other scenarios are absent from a scenario's network.  The warm start gives
+added links zero flow, as tap/tap_frankwolfe_pthread.c:564-597 inserts them.
 """
 
 from __future__ import annotations
@@ -27,7 +30,8 @@ from .solver import Solver
 from .synth import Demand, Network, Scenario
 from .tntp import read_net_mods
 
-__all__ = ["NetMod", "group_mods", "enumerate_scenarios", "apply_mods", "solve_farm"]
+__all__ = ["NetMod", "group_mods", "enumerate_scenarios", "apply_mods", "LinkBatch",
+           "build_link_batch", "solve_farm"]
 
 MAX_SUBSET_MODS = 16  # tap/tap_mpi_main.c MAXBIT
 
@@ -99,64 +103,151 @@ def apply_mods(net: Network, mods: Sequence[NetMod]) -> Network:
     return n.sort_links()
 
 
-def _capacity_only(net: Network, mods: Sequence[NetMod]):
-    """(link indices, new capacities) if the records only change capacities."""
-    links, caps = [], []
-    for m in mods:
-        if m.kind != "CHANGE":
-            return None
-        init, term, cap, length, fft, b, power, speed, toll, ltype = m.link
-        hit = np.nonzero((net.init == init) & (net.term == term))[0]
-        if len(hit) == 0:
-            raise KeyError(f"link not found for change {m.change_id}")
-        k = int(hit[0])
-        if (fft, b, power) != (net.fft[k], net.alpha[k], net.beta[k]):
-            return None
-        links.append(k)
-        caps.append(cap)
-    return np.asarray(links, np.int64), np.asarray(caps, np.float64)
+@dataclasses.dataclass
+class LinkBatch:
+    """Scenarios of link records as one batch over the union network.
+
+    union      base links (indices 0..num_base-1, base order) then each added
+               link once, in order of first appearance
+    scenarios  capacity edits per scenario (union link indices)
+    edits      per scenario (links, fft, alpha, beta) of links whose free-flow
+               time or BPR parameters differ from the union row
+    absent     per scenario, the union links its network does not have
+    members    per scenario, the union links of its network in the order the
+               reference's link array holds them after the records
+    """
+
+    union: Network
+    num_base: int
+    scenarios: List[Scenario]
+    edits: List[Tuple[np.ndarray, np.ndarray, np.ndarray, np.ndarray]]
+    absent: List[np.ndarray]
+    members: List[np.ndarray]
+
+    @property
+    def needs_links(self) -> bool:
+        """True when some scenario changes parameters or lacks a union link."""
+        return any(len(e[0]) for e in self.edits) or any(len(a) for a in self.absent)
+
+    def warm_start(self, x_base: np.ndarray) -> np.ndarray:
+        """Base flows on the base links, zero on the added ones."""
+        x = np.zeros(self.union.num_links)
+        x[: self.num_base] = x_base
+        return x
+
+    def scenario_network(self, s: int) -> Network:
+        """Scenario s's own network as the reference's farm solves it: its
+        links with their capacity and cost parameters, sorted by (init, term)
+        (the link order of scenario_order(s))."""
+        u = self.union.copy()
+        sc = self.scenarios[s]
+        for k, c in zip(sc.links.tolist(), sc.new_capacity.tolist()):
+            u.capacity[k] = c  # in record order: the last edit of a link wins
+        el, f, a, b = self.edits[s]
+        u.fft[el], u.alpha[el], u.beta[el] = f, a, b
+        return u.take(self.scenario_order(s))
+
+    def scenario_order(self, s: int) -> np.ndarray:
+        """Union link index of each link of scenario_network(s), in its order."""
+        mem = self.members[s]
+        u = self.union
+        return mem[np.lexsort((u.term[mem], u.init[mem]))]
+
+
+_FIELDS = ("init", "term", "capacity", "length", "fft", "alpha", "beta", "speed", "toll",
+           "link_type")
+
+
+def build_link_batch(net: Network, scen_recs: Sequence[Tuple[str, Sequence[NetMod]]]
+                     ) -> LinkBatch:
+    """Union network and per-scenario edits for scenarios given as (id, records),
+    the records applied in order as tap/tap_mpi_main.c:201-240 applies them:
+    ADD appends a link, CHANGE replaces the record of the first link (in the
+    scenario's link order) with the same end nodes."""
+    M = net.num_links
+    added: Dict[int, int] = {}  # id(record) -> union link
+    add_rows: List[Tuple] = []
+    for _, recs in scen_recs:
+        for m in recs:
+            if m.kind == "ADD" and id(m) not in added:
+                added[id(m)] = M + len(add_rows)
+                add_rows.append(m.link)
+            elif m.kind not in ("ADD", "CHANGE"):
+                raise ValueError(f"bad modification type {m.kind}")
+    union = net.copy()
+    if add_rows:
+        cols = list(zip(*add_rows))
+        for f, vals in zip(_FIELDS, cols):
+            arr = getattr(union, f)
+            setattr(union, f, np.concatenate([arr, np.asarray(vals, dtype=arr.dtype)]))
+    U = union.num_links
+    all_added = np.arange(M, U, dtype=np.int64)
+    scen, edits, absent, members = [], [], [], []
+    for sid, recs in scen_recs:
+        links = list(range(M))  # this scenario's link array, in the reference's order
+        cap_l, cap_v = [], []
+        par: Dict[int, Tuple[float, float, float]] = {}
+        mine = []
+        for m in recs:
+            init, term, cap, length, fft, b, power, speed, toll, ltype = m.link
+            if m.kind == "ADD":
+                u = added[id(m)]
+                links.append(u)
+                mine.append(u)
+                par.pop(u, None)  # an added link starts from its own record
+                continue
+            u = next((k for k in links if union.init[k] == init and union.term[k] == term), None)
+            if u is None:
+                raise KeyError(f"link not found for change {m.change_id}")
+            cap_l.append(u)
+            cap_v.append(cap)
+            par[u] = (fft, b, power)
+        el = np.asarray([u for u, p in par.items()
+                         if p != (union.fft[u], union.alpha[u], union.beta[u])], np.int64)
+        edits.append((el, np.asarray([par[u][0] for u in el], np.float64),
+                      np.asarray([par[u][1] for u in el], np.float64),
+                      np.asarray([par[u][2] for u in el], np.float64)))
+        scen.append(Scenario(sid, np.asarray(cap_l, np.int64), np.asarray(cap_v, np.float64)))
+        absent.append(np.setdiff1d(all_added, np.asarray(mine, np.int64)))
+        members.append(np.asarray(links, np.int64))
+    return LinkBatch(union, M, scen, edits, absent, members)
 
 
 def solve_farm(net: Network, dem: Demand, mods_path: str, mode: str = "single",
                changelist: Optional[str] = None, target_relgap: float = 1e-4,
                max_iters: int = 0, warm_start: bool = True, base_relgap: float = 1e-5,
                precision: str = "fp32", solver: Optional[Solver] = None):
-    """Solve every scenario of a net-mods file; returns a list of dicts
-    (id, total_cost = VHT, relgap, iterations, batched flag)."""
+    """Solve every scenario of a net-mods file in one batch; returns a list of
+    dicts (id, total_cost = VHT, relgap, iterations, batched flag)."""
     raw = read_net_mods(mods_path)
     mods = [NetMod(c, k, l, p) for c, k, l, p in raw]
     groups = group_mods(mods)
     scen = enumerate_scenarios(list(groups), mode, changelist)
+    batch = build_link_batch(net, [(sid, [m for c in sel for m in groups[c]])
+                                   for sid, sel in scen])
     own = solver is None
     s = solver or Solver(net, dem, precision=precision)
+    su = None
     try:
         x0 = None
         if warm_start:
             s.solve(target_relgap=base_relgap, max_iters=max_iters or 100000)
-            x0 = s.flows()[0]
-        batch, batch_ids, others = [], [], []
-        for sid, sel in scen:
-            recs = [m for c in sel for m in groups[c]]
-            co = _capacity_only(net, recs)
-            if co is None:
-                others.append((sid, recs))
-            else:
-                batch.append(Scenario(sid, co[0], co[1]))
-                batch_ids.append(sid)
-        out = []
-        if batch:
-            res = s.solve_scenarios(batch, max_iters=max_iters, target_relgap=target_relgap,
-                                    x0=x0)
-            for sid, r in zip(batch_ids, res):
-                out.append(dict(id=sid, batched=True, **r))
-        for sid, recs in others:
-            n2 = apply_mods(net, recs)
-            with Solver(n2, dem, precision=precision) as s2:
-                r = s2.solve(max_iters=max_iters, target_relgap=target_relgap)
-            out.append(dict(id=sid, batched=False, **r))
-        order = {sid: i for i, (sid, _) in enumerate(scen)}
-        out.sort(key=lambda d: order[d["id"]])
-        return out
+            x0 = batch.warm_start(s.flows()[0])
+        # the union network differs from the base only when records add links
+        if batch.union.num_links != net.num_links:
+            su = Solver(batch.union, dem, precision=precision)
+        sv = su or s
+        if batch.needs_links:
+            sv.set_scenario_links(batch.edits, batch.absent)
+        try:
+            res = sv.solve_scenarios(batch.scenarios, max_iters=max_iters,
+                                     target_relgap=target_relgap, x0=x0)
+        finally:
+            if batch.needs_links:
+                sv.set_scenario_links(None)
+        return [dict(id=sid, batched=True, **r) for (sid, _), r in zip(scen, res)]
     finally:
+        if su is not None:
+            su.close()
         if own:
             s.close()

@@ -175,6 +175,51 @@ class Solver:
         K.check(self.L.tapgpu_aon(self.h, K.ptr(w, K.F64P), K.ptr(y, K.F64P)))
         return y
 
+    def set_scenario_links(self, edits: Optional[Sequence] = None,
+                           absent: Optional[Sequence] = None):
+        """Per-scenario link records for the following solve_scenarios calls
+        (the context's network is the union of every scenario's links).
+
+        edits[s]: (links, fft, alpha, beta) arrays of scenario s's changed
+        link parameters; absent[s]: the links scenario s's network does not
+        have.  None returns to the one base network."""
+        if edits is None and absent is None:
+            K.check(self.L.tapgpu_set_scenario_links(self.h, 0, None, None, None, None, None,
+                                                     None, None))
+            return
+        S = len(edits) if edits is not None else len(absent)
+        edits = edits if edits is not None else [None] * S
+        absent = absent if absent is not None else [None] * S
+        if len(edits) != S or len(absent) != S:
+            raise ValueError("edits and absent must list the same scenarios")
+        cols = [[], [], [], []]
+        eptr = np.zeros(S + 1, np.int64)
+        aptr = np.zeros(S + 1, np.int64)
+        alist = []
+        for i in range(S):
+            e = edits[i]
+            n = 0
+            if e is not None:
+                arrs = [np.atleast_1d(np.asarray(a)) for a in e]
+                n = len(arrs[0])
+                if any(len(a) != n for a in arrs):
+                    raise ValueError("edit arrays of one scenario differ in length")
+                for c, a in zip(cols, arrs):
+                    c.append(a)
+            eptr[i + 1] = eptr[i] + n
+            a = np.zeros(0, np.int64) if absent[i] is None else np.asarray(absent[i], np.int64)
+            alist.append(a)
+            aptr[i + 1] = aptr[i] + len(a)
+        cat = [np.ascontiguousarray(np.concatenate(c) if c else np.zeros(0), t)
+               for c, t in zip(cols, (np.int64, np.float64, np.float64, np.float64))]
+        al = np.ascontiguousarray(np.concatenate(alist) if alist else np.zeros(0), np.int64)
+        keep = [np.zeros(1, np.int64) if a.size == 0 else a for a in (cat[0], al)]
+        fv = [np.zeros(1) if a.size == 0 else a for a in cat[1:]]
+        K.check(self.L.tapgpu_set_scenario_links(
+            self.h, S, K.ptr(eptr, K.I64P), K.ptr(keep[0], K.I64P), K.ptr(fv[0], K.F64P),
+            K.ptr(fv[1], K.F64P), K.ptr(fv[2], K.F64P), K.ptr(aptr, K.I64P),
+            K.ptr(keep[1], K.I64P)))
+
     def set_scenario_demand(self, demand: Optional[np.ndarray]):
         """Per-scenario OD demand [S][nnz] (entries in the order of the Demand
         given at construction) for the following solve_scenarios calls; None
