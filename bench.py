@@ -12,10 +12,17 @@ the warm-start flows in; the capacity rows are made on the device) and
 tapgpu_get_link_flows_batch (every scenario's flows and costs out).
 
 Also reported: scenarios/sec to relative gap 1e-4 for the batched solver and
-for the plain single-scenario GPU path, the roofline of the dominant kernel
-(all-origins shortest paths), per-kernel times measured with CUDA events on
-the solver's stream, SM clocks sampled during the timed region, and the CPU
-baseline (the oracle's pthread Frank-Wolfe on the host cores).
+for the plain single-scenario GPU path, the VHT change of each upgrade
+(batched against individual plain solves), the same workload in FP64 mode
+(``fp64_mode``), FW iterations/sec of the plain path on the 24-, 416- and
+10,000-node networks in both precisions with the oracle on the host cores
+beside them (``configs``), the FP32-path error against FP64 on each
+(``precision_error``), the adjoint on the 10k- and 100k-node networks, the
+roofline of the dominant kernel (all-origins shortest paths), per-kernel
+times measured with CUDA events on the solver's stream, SM clocks sampled
+during the timed region, and the CPU baseline (the oracle's pthread
+Frank-Wolfe on the host cores).  ``--no-extras`` / ``--no-cpu`` skip the
+extra measurements / the host-core legs.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -231,6 +238,75 @@ def run_reference(args, rank, world):
     return 0
 
 
+def cpu_config_rows(cores):
+    """The oracle's pthread FW (the reference's algorithm, all host threads) on
+    C1-C3: FW iterations per second on a bounded sample of each."""
+    import oracle
+    from traffic_assignment_gb300 import synth
+    rows = {}
+    for name, maker, iters in (("C1", synth.make_small24, 100), ("C2", synth.make_grid416, 2000),
+                               ("C3", synth.make_grid10k, 20)):
+        net, dem = maker()
+        t0 = time.perf_counter()
+        r = oracle.frankwolfe(net, dem, threads=cores, max_iters=iters)
+        wall = time.perf_counter() - t0
+        loop_s = float(np.sum(r["trace"][:, 6])) / 1e3
+        rows[name] = {"fw_iterations_per_s": iters / loop_s, "iterations": iters,
+                      "wall_s": wall, "threads": cores}
+    return rows
+
+
+def _plain_solve(net, dem, precision, iters=0, relgap=0.0):
+    """One plain (single-scenario) GPU solve after an untimed warm-up solve:
+    wall-clock iterations per second through Solver.solve, and the result."""
+    import torch
+
+    from traffic_assignment_gb300 import Solver
+    with Solver(net, dem, precision=precision) as s:
+        s.solve(max_iters=5)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = s.solve(max_iters=iters, target_relgap=relgap)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        x, _ = s.flows()
+    return {"iterations": r["iterations"], "fw_iterations_per_s": r["iterations"] / wall,
+            "ms_per_iteration": 1e3 * wall / max(1, r["iterations"]), "relgap": r["relgap"],
+            "vht": r["total_cost"]}, r, x
+
+
+def _errors(x32, r32, x64, r64):
+    """FP32-path result against the FP64 one (the FP64 GPU path equals the
+    all-FP64 oracle to ~1e-10 in the GPU tests): link flows relative to the
+    largest flow, VHT, objective and relative gap relative to the FP64 value."""
+    def rv(a, b):
+        return abs(a - b) / abs(b) if b else abs(a - b)
+    return {"flow_max": float(np.abs(x32 - x64).max() / max(1.0, np.abs(x64).max())),
+            "flow_l1": float(np.abs(x32 - x64).sum() / max(1e-300, np.abs(x64).sum())),
+            "vht": rv(r32["total_cost"], r64["total_cost"]),
+            "objective": rv(r32["objective"], r64["objective"]),
+            "relgap": rv(r32["relgap"], r64["relgap"])}
+
+
+def gpu_config_rows():
+    """C1-C3 on the plain single-scenario GPU path in both precisions, and the
+    FP32-path error against FP64 on each."""
+    from traffic_assignment_gb300 import synth
+    rows, errs = {}, {}
+    for name, maker, iters, relgap in (("C1", synth.make_small24, 100, 0.0),
+                                       ("C2", synth.make_grid416, 0, 1e-5),
+                                       ("C3", synth.make_grid10k, 500, 0.0)):
+        net, dem = maker()
+        row64, r64, x64 = _plain_solve(net, dem, "fp64", iters, relgap)
+        row32, r32, x32 = _plain_solve(net, dem, "fp32", iters, relgap)
+        rows[name] = {"network": f"{net.num_nodes} nodes, {net.num_links} links, "
+                                 f"{net.num_zones} zones",
+                      "stop": f"{iters} iterations" if iters else f"relative gap {relgap:g}",
+                      "fp64": row64, "fp32_paths": row32}
+        errs[name] = dict(_errors(x32, r32, x64, r64), compared=rows[name]["stop"])
+    return rows, errs
+
+
 def adjoint_check(net, dem, iters=50):
     """dVHT/dcapacity on the 10k-node network after `iters` FW iterations (FP32
     paths, exact line search): GPU forward and adjoint times.  Its accuracy is
@@ -255,6 +331,61 @@ def adjoint_check(net, dem, iters=50):
             "grad_nonzero_links": int(np.count_nonzero(g)),
             "accuracy": "tests/test_gpu_adjoint.py: 1e-9 of max |g| vs the FP64 CPU reverse "
                         "sweep; 1e-3 vs central differences (1% step) on 64 random links"}
+
+
+def adjoint_large(iters=50):
+    """C5 throughput: dVHT/dcapacity of the 100k-node network (99,856 nodes,
+    ~400k links, 4,000 zones) through `iters` FW iterations, FP32 paths and an
+    FP64 adjoint; forward (with the tape) and reverse sweep timed apart."""
+    import torch
+
+    from traffic_assignment_gb300 import Solver, synth
+    net, dem = synth.make_grid100k()
+    with Solver(net, dem, precision="fp32", record_tape=True, tape_capacity=iters,
+                line_search="exact") as s:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.solve(max_iters=iters)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        vht, g = s.adjoint_vht()
+        t2 = time.perf_counter()
+    return {"network": "grid100k: 99,856 nodes, %d links, 4,000 zones" % net.num_links,
+            "iterations": iters, "forward_ms": 1e3 * (t1 - t0), "adjoint_ms": 1e3 * (t2 - t1),
+            "gradient_links_per_s": net.num_links / (t2 - t1), "vht": vht,
+            "grad_nonzero_links": int(np.count_nonzero(g))}
+
+
+def fp64_batched(net, dem, scen, xb, steps, warmup, x32_batch, res32):
+    """The same C4 workload in FP64 mode (all-FP64 shortest paths, the
+    reference's arithmetic): device-timed scenario-FW-iterations/s, and the
+    FP32-path error over every scenario after the same warm-started
+    iterations (x32_batch / res32: the FP32 run's flows and results)."""
+    import torch
+
+    from traffic_assignment_gb300 import Solver
+    K = len(res32) and res32[0]["iterations"]
+    with Solver(net, dem, precision="fp64") as s:
+        res = s.solve_scenarios(scen, max_iters=K, x0=xb)
+        x64, _ = s.flows_batch(0, len(scen))
+        s.run_iterations(warmup)
+        stream = torch.cuda.ExternalStream(s.stream_ptr())
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        s.run_iterations(steps)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+    worst = {}
+    for i in range(len(scen)):
+        e = _errors(x32_batch[i], res32[i], x64[i], res[i])
+        for k, v in e.items():
+            worst[k] = max(worst.get(k, 0.0), v)
+    worst["compared"] = f"all {len(scen)} scenarios after {K} warm-started iterations"
+    return {"value": len(scen) / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "steps": steps,
+            "dtype": "f64"}, worst
 
 
 def large_network_rate(iters=6):
@@ -304,13 +435,14 @@ def run_ours(args, rank, world, local_rank):
     # plain single-scenario path: a few scenarios one at a time to rel-gap 1e-4
     plain_n = min(args.plain_scenarios, S)
     t0 = time.perf_counter()
-    plain_iters = []
+    plain_iters, plain_vht = [], []
     for sc in scen[:plain_n]:
         cap = net.capacity.copy()
         cap[sc.links] = sc.new_capacity
         solver.set_capacity(cap)
         q = solver.solve(target_relgap=1e-4, max_iters=args.max_iters, x0=xb)
         plain_iters.append(q["iterations"])
+        plain_vht.append(q["total_cost"])
     plain_s = time.perf_counter() - t0
     solver.set_capacity(net.capacity)
     plain_sps = plain_n / plain_s
@@ -379,12 +511,38 @@ def run_ours(args, rank, world, local_rank):
     per_task = profile_traffic()
     traffic = None if per_task is None else per_task * tasks_per_launch
 
+    # VHT change of each upgrade (the reference farm's output): batched solves
+    # against the plain path's individual solves of the same scenarios
+    base_vht = base["total_cost"]
+    dv_b = np.array([q["total_cost"] - base_vht for q in res])
+    dv_p = np.array(plain_vht) - base_vht
+    vht_change = {
+        "base_vht": base_vht,
+        "batched_delta_vht": {"mean": float(dv_b.mean()), "min": float(dv_b.min()),
+                              "max": float(dv_b.max()), "scenarios": S},
+        "plain_subset": [{"scenario": scen[i].change_id, "delta_vht_batched": float(dv_b[i]),
+                          "delta_vht_plain": float(dv_p[i])} for i in range(plain_n)],
+        "max_abs_diff_rel_base_vht": float(np.max(np.abs(dv_b[:plain_n] - dv_p)) / base_vht),
+    }
+
     line = None
     if rank == 0:
         clocks = clk.summary()
         cpu = cpu_baseline(net, dem, scen[0], seconds=args.cpu_seconds) if not args.no_cpu else None
+        cpu_rows = cpu_config_rows(os.cpu_count() or 1) if not args.no_cpu else None
         adj = None if args.no_extras else adjoint_check(net, dem)
         large = None if args.no_extras else large_network_rate()
+        fp64 = rows = adj_large = None
+        prec = {}
+        if not args.no_extras:
+            # FP32 paths and FP64 on the same warm-started C4 iterations
+            res30 = solver.solve_scenarios(scen, max_iters=30, x0=xb)
+            x30, _ = solver.flows_batch(0, S)
+            fp64, prec["C4"] = fp64_batched(net, dem, scen, xb, args.steps, args.warmup, x30,
+                                            res30)
+            rows, errs = gpu_config_rows()
+            prec.update(errs)
+            adj_large = adjoint_large()
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -430,7 +588,12 @@ def run_ours(args, rank, world, local_rank):
                             "tapgpu_get_link_flows_batch (all scenarios' volumes and costs)",
                     "iterations": e2e_iters},
             "gpu_launches": tm["kernel_launches"],
+            "fp64_mode": fp64,
+            "vht_change": vht_change,
+            "configs": {"gpu": rows, "cpu_port": cpu_rows},
+            "precision_error": prec or None,
             "adjoint": adj,
+            "adjoint_large": adj_large,
             "large_network": large,
         }
         print(json.dumps(line), flush=True)

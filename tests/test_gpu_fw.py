@@ -46,7 +46,7 @@ def test_aon_matches_oracle(built_lib, grid416):
             assert _rel(y, ref) < 1e-12
 
 
-VARIANTS = ["rounds", "async", "nearfar", "nearfar_queue"]
+VARIANTS = ["rounds", "async", "nearfar", "nearfar_queue", "bucket"]
 
 
 @pytest.mark.parametrize("variant", VARIANTS)
@@ -269,3 +269,40 @@ def test_large_network(built_lib, large_network_reference, precision):
     assert np.abs(x - ref["x"]).sum() <= 1e-3 * np.abs(ref["x"]).sum()
     y_ref = oracle.aon(net, dem, ref["t"], threads=os.cpu_count() or 1)
     assert abs(ref["t"] @ y - ref["t"] @ y_ref) <= RTOL64 * (ref["t"] @ y_ref)
+
+
+@pytest.mark.parametrize("case", ["grid416", "grid3600", "grid3600_global", "grid10k_batch",
+                                  "grid416_wide_delta"])
+def test_bucket_kernel_equals_queue_kernel(built_lib, case):
+    """The barrier-synchronous bucket kernel and the queue kernel reach the same
+    least fixed point of the FP32 relaxations, so labels, trees and flows are
+    bit-identical: single scenarios, labels in global memory, a batch of
+    warm-started scenarios, and a threshold step so wide that the whole graph
+    is one near set (rounds then outgrow the ring and scan the bitmap)."""
+    kw = {}
+    if case.startswith("grid416"):
+        net, dem = synth.make_grid416()
+    elif case.startswith("grid3600"):
+        net, dem = synth.make_grid3600()
+        kw["global_scratch"] = case.endswith("global")
+    else:
+        net, dem = synth.make_grid10k()
+    if case == "grid416_wide_delta":
+        kw["nf_delta"] = 1e9
+    outs = {}
+    for variant in ("nearfar_queue", "bucket"):
+        with Solver(net, dem, precision="fp32", sssp_variant=variant, **kw) as s:
+            if case == "grid10k_batch":
+                s.solve(max_iters=6)
+                x0, _ = s.flows()
+                scen = synth.make_scenarios(net, 12)
+                res = s.solve_scenarios(scen, max_iters=5, x0=x0)
+                x, t = s.flows_batch(0, len(scen))
+                outs[variant] = (x, t, [q["relgap"] for q in res])
+            else:
+                r = s.solve(max_iters=15)
+                x, t = s.flows()
+                outs[variant] = (x, t, [r["relgap"]])
+    np.testing.assert_array_equal(outs["bucket"][0], outs["nearfar_queue"][0])
+    np.testing.assert_array_equal(outs["bucket"][1], outs["nearfar_queue"][1])
+    assert outs["bucket"][2] == outs["nearfar_queue"][2]
