@@ -46,7 +46,7 @@ def test_aon_matches_oracle(built_lib, grid416):
             assert _rel(y, ref) < 1e-12
 
 
-VARIANTS = ["rounds", "async", "nearfar", "nearfar_queue", "bucket"]
+VARIANTS = ["rounds", "async", "nearfar", "nearfar_queue"]
 
 
 @pytest.mark.parametrize("variant", VARIANTS)
@@ -272,13 +272,14 @@ def test_large_network(built_lib, large_network_reference, precision):
 
 
 @pytest.mark.parametrize("case", ["grid416", "grid3600", "grid3600_global", "grid10k_batch",
-                                  "grid416_wide_delta"])
-def test_bucket_kernel_equals_queue_kernel(built_lib, case):
-    """The barrier-synchronous bucket kernel and the queue kernel reach the same
-    least fixed point of the FP32 relaxations, so labels, trees and flows are
-    bit-identical: single scenarios, labels in global memory, a batch of
-    warm-started scenarios, and a threshold step so wide that the whole graph
-    is one near set (rounds then outgrow the ring and scan the bitmap)."""
+                                  "grid416_wide_delta", "grid416_narrow_delta"])
+def test_queue_kernel_equals_near_far_kernel(built_lib, case):
+    """The queue kernel (its far set read off the labels at each phase step)
+    and the bitmap near-far kernel reach the same least fixed point of the
+    FP32 relaxations, so labels, trees and flows are bit-identical: single
+    scenarios, labels in global memory, a batch of warm-started scenarios, and
+    threshold steps so wide that the whole graph is one near set (the ring
+    overflows into the bitmap) or so narrow that most phases hold few nodes."""
     kw = {}
     if case.startswith("grid416"):
         net, dem = synth.make_grid416()
@@ -289,8 +290,10 @@ def test_bucket_kernel_equals_queue_kernel(built_lib, case):
         net, dem = synth.make_grid10k()
     if case == "grid416_wide_delta":
         kw["nf_delta"] = 1e9
+    if case == "grid416_narrow_delta":
+        kw["nf_delta"] = 0.05 * float(np.mean(net.fft))
     outs = {}
-    for variant in ("nearfar_queue", "bucket"):
+    for variant in ("nearfar", "nearfar_queue"):
         with Solver(net, dem, precision="fp32", sssp_variant=variant, **kw) as s:
             if case == "grid10k_batch":
                 s.solve(max_iters=6)
@@ -303,6 +306,6 @@ def test_bucket_kernel_equals_queue_kernel(built_lib, case):
                 r = s.solve(max_iters=15)
                 x, t = s.flows()
                 outs[variant] = (x, t, [r["relgap"]])
-    np.testing.assert_array_equal(outs["bucket"][0], outs["nearfar_queue"][0])
-    np.testing.assert_array_equal(outs["bucket"][1], outs["nearfar_queue"][1])
-    assert outs["bucket"][2] == outs["nearfar_queue"][2]
+    np.testing.assert_array_equal(outs["nearfar_queue"][0], outs["nearfar"][0])
+    np.testing.assert_array_equal(outs["nearfar_queue"][1], outs["nearfar"][1])
+    assert outs["nearfar_queue"][2] == outs["nearfar"][2]

@@ -1220,314 +1220,6 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
   }
 }
 
-// ---------------------------------------------------------------------------
-// k_sssp_bkt: barrier-synchronous near-far with one lane per (node, out-link)
-// ---------------------------------------------------------------------------
-//
-// The near set below a threshold is corrected in rounds: the nodes queued for
-// a round sit in a ring of shared memory; warps claim eight of them at a time
-// and four lanes expand each node, one padded {head, weight} record per lane
-// (one 32-byte load per node), so a warp relaxes 32 links with one label
-// atomic per lane.  Heads that enter the near set are appended to the ring
-// for the next round, one ring reservation per warp.  Two barriers end a
-// round; no warp ever waits on another warp's slot, counter or flag.  When
-// the round finds nothing left, the phase step (as k_sssp_nfq's) raises the
-// threshold to the smallest far label + delta and queues the far nodes below
-// it.  The near bitmap is the truth and the ring an index into it: a claim
-// clears the node's bit (a node queued twice is expanded once per set bit),
-// and an append that finds the ring full leaves its node in the bitmap, which
-// the next round then scans word by word.  FP32 path costs only (padded
-// records); R holds node ids (16 bits up to 65,535 nodes, else 32).
-constexpr int kBCap = 1024;  // ring slots (a power of two; as kQCap, so FP64 labels can run k_sssp_nfq)
-static_assert(kBCap == kQCap, "the bucket and queue kernels share one scratch layout");
-
-template <int BLOCK, bool SMEM, typename R>
-__global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) k_sssp_bkt(PathArgs a) {
-  using U = unsigned;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ int sh_task;
-  __shared__ unsigned qtail, claim, next_end;
-  __shared__ int ovf_next, bm_flag;
-  __shared__ U sh_min;
-  constexpr bool kDeg16 = std::is_same<R, unsigned short>::value;
-  constexpr unsigned kHead = kDeg16 ? 0xffffu : 0xffffffffu;
-  constexpr int kWarps = BLOCK / 32;
-  const int n1 = a.g.n1;
-  const int nwords = (n1 + 31) >> 5;
-  unsigned char* base =
-      SMEM ? smem_raw
-           : static_cast<unsigned char*>(a.scratch) + static_cast<size_t>(blockIdx.x) * a.scratch_stride;
-  U* dist = reinterpret_cast<U*>(base);
-  unsigned* near = reinterpret_cast<unsigned*>(base + align16(sizeof(U) * n1));
-  unsigned* far = near + nwords;
-  R* ring = reinterpret_cast<R*>(far + nwords);
-  const int lane = threadIdx.x & 31;
-  const int warp = threadIdx.x >> 5;
-  const int grp = lane >> 2, slot4 = lane & 3;
-  const unsigned lt_mask = (1u << lane) - 1u;
-  const int F = a.g.first_thru;
-  const int my_words = warp < nwords ? (nwords - warp + kWarps - 1) / kWarps : 0;
-  const float delta = static_cast<float>(a.nf_delta);
-
-  for (;;) {
-    __syncthreads();
-    if (threadIdx.x == 0) sh_task = atomicAdd(a.counter, 1) + a.task_begin;
-    __syncthreads();
-    const int task = sh_task;
-    if (task >= a.task_end) break;
-    const int tslot = task / a.num_sources;
-    const int scen = a.scen_list ? a.scen_list[tslot] : 0;
-    if (a.state && a.state[scen].done) continue;
-    const int src = a.sources[task - tslot * a.num_sources];
-    const uint2* e4s = a.e4 + static_cast<size_t>(scen) * n1 * 4;
-    const uint2* ecsr = a.e32 + static_cast<size_t>(scen) * a.g.m;
-    unsigned expanded = 0, batches = 0;
-    int phases = 0, rounds = 0;
-
-    for (int v = threadIdx.x; v < n1; v += BLOCK) dist[v] = DT<float>::kInf;
-    for (int i = threadIdx.x; i < 2 * nwords; i += BLOCK) near[i] = 0u;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      dist[src] = 0u;
-      near[src >> 5] = 1u << (src & 31);
-      ring[0] = static_cast<R>(src);
-      qtail = 1u;
-      claim = 0u;
-      ovf_next = 0;
-      bm_flag = 0;
-    }
-    __syncthreads();
-    unsigned rh = 0u, rt = 1u;  // this round's ring entries [rh, rt)
-    bool rbm = false;           // this round also scans the near bitmap
-    U thr = __float_as_uint(delta);
-
-    // Relax link (h, w) from label du; returns 1 when h newly enters the near set.
-    auto relax = [&](int h, float w, float du) -> bool {
-      const U nb = __float_as_uint(__fadd_rn(du, w));
-      const U old = atomicMin(dist + h, nb);
-      if (nb < old && !(h < F && h != src)) {
-        const unsigned bit = 1u << (h & 31);
-        if (nb < thr) return !(atomicOr(near + (h >> 5), bit) & bit);
-        atomicOr(far + (h >> 5), bit);
-      }
-      return false;
-    };
-    // Queue the heads that entered the near set, one ring reservation per warp;
-    // past the ring's room they stay in the bitmap for the next round's scan.
-    auto append = [&](bool app, int h) {
-      const unsigned m = __ballot_sync(kFull, app);
-      if (!m) return;
-      const int leader = __ffs(m) - 1;
-      unsigned pos = 0u;
-      if (lane == leader) pos = atomicAdd(&qtail, static_cast<unsigned>(__popc(m)));
-      pos = __shfl_sync(kFull, pos, leader);
-      if (app) {
-        const unsigned p = pos + static_cast<unsigned>(__popc(m & lt_mask));
-        if (p - rh < static_cast<unsigned>(kBCap))
-          ring[p & (kBCap - 1)] = static_cast<R>(h);
-        else
-          ovf_next = 1;
-      }
-    };
-    // Expand the node of each four-lane group (v valid in the whole group).
-    auto expand = [&](int v, bool valid) {
-      const bool ex = valid && !(v < F && v != src);  // zones are never passed through
-      int deg = 0;
-      uint2 r = make_uint2(0u, 0u);
-      float du = 0.f;
-      if (ex) {
-        r = __ldg(e4s + static_cast<size_t>(v) * 4 + slot4);
-        if constexpr (kDeg16) {
-          deg = static_cast<int>(r.x >> 16);
-        } else {
-          deg = __ldg(a.g.out_deg + v);
-        }
-        du = __uint_as_float(dist[v]);
-      }
-      const int h0 = static_cast<int>(r.x & kHead);
-      const bool app0 = slot4 < deg && relax(h0, __uint_as_float(r.y), du);
-      append(app0, h0);
-      // further links of nodes with more than four (rare on road networks)
-      int row = -1;
-      for (int e = 4;; e += 4) {
-        const bool has = ex && e + slot4 < deg;
-        if (!__any_sync(kFull, has)) break;
-        bool app = false;
-        int h = 0;
-        if (has) {
-          if (row < 0) row = __ldg(a.g.row_ptr + v);
-          const uint2 q = __ldg(ecsr + row + e + slot4);
-          h = static_cast<int>(q.x);
-          app = relax(h, __uint_as_float(q.y), du);
-        }
-        append(app, h);
-      }
-      expanded += (valid && slot4 == 0) ? 1u : 0u;
-    };
-
-    for (;;) {    // phases
-      for (;;) {  // rounds
-        if (rh == rt && !rbm) break;
-        if (++rounds > 64 * (n1 + 2)) {
-          if (threadIdx.x == 0) atomicOr(a.err, kErrRounds);
-          break;
-        }
-        // -- the ring's entries of this round, eight nodes per warp at a time ----
-        for (;;) {
-          unsigned c = 0u;
-          if (lane == 0) c = atomicAdd(&claim, 8u);
-          c = __shfl_sync(kFull, c, 0);
-          if (c >= rt - rh) break;
-          const unsigned idx = rh + c + static_cast<unsigned>(grp);
-          int v = 0;
-          bool valid = false;
-          if (slot4 == 0 && idx - rh < rt - rh) {
-            v = static_cast<int>(ring[idx & (kBCap - 1)]);
-            const unsigned bit = 1u << (v & 31);
-            valid = (atomicAnd(near + (v >> 5), ~bit) & bit) != 0u;
-          }
-          v = __shfl_sync(kFull, v, lane & ~3);
-          valid = __shfl_sync(kFull, valid, lane & ~3);
-          ++batches;
-          expand(v, valid);
-        }
-        // -- nodes the ring had no room for: this warp's bitmap words -----------
-        if (rbm) {
-          for (int j0 = 0; j0 < my_words; j0 += 32) {
-            const int j = j0 + lane;
-            const int wi = warp + j * kWarps;
-            unsigned word = 0u;
-            if (j < my_words) {
-              word = near[wi];
-              if (word) word = atomicExch(near + wi, 0u);
-            }
-            const int cnt = __popc(word);
-            int incl = cnt;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-              const int y = __shfl_up_sync(kFull, incl, o);
-              if (lane >= o) incl += y;
-            }
-            const int total = __shfl_sync(kFull, incl, 31);
-            for (int b = 0; b < total; b += 8) {
-              const int jj = b + grp;
-              int owner = 0;
-#pragma unroll
-              for (int step = 16; step >= 1; step >>= 1) {
-                const int probe = __shfl_sync(kFull, incl, owner + step - 1);
-                if (probe <= jj) owner += step;
-              }
-              owner &= 31;
-              const unsigned ow = __shfl_sync(kFull, word, owner);
-              const int oincl = __shfl_sync(kFull, incl, owner);
-              const bool valid = jj < total;
-              int v = 0;
-              if (valid)
-                v = ((warp + (j0 + owner) * kWarps) << 5) + nth_set_bit(ow, jj - (oincl - __popc(ow)));
-              ++batches;
-              expand(v, valid);
-            }
-          }
-        }
-        // -- end of round: the appended entries become the next round -----------
-        __syncthreads();
-        if (threadIdx.x == 0) {
-          unsigned t = qtail;
-          if (t - rh > static_cast<unsigned>(kBCap)) t = rh + static_cast<unsigned>(kBCap);
-          qtail = t;
-          next_end = t;
-          claim = 0u;
-          bm_flag = ovf_next;
-          ovf_next = 0;
-        }
-        __syncthreads();
-        rh = rt;
-        rt = next_end;
-        rbm = bm_flag != 0;
-      }
-      // -- phase step: threshold = smallest far label + delta ---------------------
-      if (threadIdx.x == 0) sh_min = DT<float>::kInf;
-      __syncthreads();
-      U mn = DT<float>::kInf;
-      for (int i = threadIdx.x; i < nwords; i += BLOCK) {
-        const unsigned w = far[i];
-        if (!w) continue;
-        unsigned keep = 0u, ww = w;
-        while (ww) {
-          const int bpos = __ffs(ww) - 1;
-          ww &= ww - 1;
-          const U dv = dist[(i << 5) + bpos];
-          if (dv >= thr) {
-            keep |= 1u << bpos;
-            if (dv < mn) mn = dv;
-          }
-        }
-        if (keep != w) far[i] = keep;
-      }
-      if (mn != DT<float>::kInf) atomicMin(&sh_min, mn);
-      __syncthreads();
-      const U fmin = sh_min;
-      if (fmin == DT<float>::kInf) break;  // nothing left: labels are final
-      if (++phases > a.max_rounds) {
-        if (threadIdx.x == 0) atomicOr(a.err, kErrRounds);
-        break;
-      }
-      thr = __float_as_uint(__fadd_rn(__uint_as_float(fmin), delta));
-      if (thr <= fmin) thr = fmin + 1;
-      for (int i = threadIdx.x; i < nwords; i += BLOCK) {
-        const unsigned w = far[i];
-        if (!w) continue;
-        unsigned take = 0u, ww = w;
-        while (ww) {
-          const int bpos = __ffs(ww) - 1;
-          ww &= ww - 1;
-          if (dist[(i << 5) + bpos] < thr) take |= 1u << bpos;
-        }
-        if (!take) continue;
-        far[i] = w & ~take;
-        near[i] = take;
-        unsigned p = atomicAdd(&qtail, static_cast<unsigned>(__popc(take)));
-        while (take) {
-          const int bpos = __ffs(take) - 1;
-          take &= take - 1;
-          if (p - rh < static_cast<unsigned>(kBCap))
-            ring[p & (kBCap - 1)] = static_cast<R>((i << 5) + bpos);
-          else
-            ovf_next = 1;
-          ++p;
-        }
-      }
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        unsigned t = qtail;
-        if (t - rh > static_cast<unsigned>(kBCap)) t = rh + static_cast<unsigned>(kBCap);
-        qtail = t;
-        next_end = t;
-        claim = 0u;
-        bm_flag = ovf_next;
-        ovf_next = 0;
-      }
-      __syncthreads();
-      rt = next_end;
-      rbm = bm_flag != 0;
-    }
-    float* out = static_cast<float*>(a.dist) + static_cast<size_t>(task - a.task_begin) * n1;
-    for (int v = threadIdx.x; v < n1; v += BLOCK) out[v] = __uint_as_float(dist[v]);
-    if (a.stats) {
-      expanded = warp_sum(static_cast<int>(expanded));
-      if (lane == 0) {
-        atomicAdd(a.stats + 2, static_cast<unsigned long long>(expanded));
-        atomicAdd(a.stats + 4, static_cast<unsigned long long>(batches));
-      }
-      if (threadIdx.x == 0) {
-        atomicAdd(a.stats + 0, static_cast<unsigned long long>(rounds));
-        atomicAdd(a.stats + 1, 1ull);
-        atomicAdd(a.stats + 3, static_cast<unsigned long long>(phases));
-      }
-    }
-  }
-}
-
 constexpr unsigned short kNoParent16 = 0xffffu;  // node ids are below 65535 in the compact layout
 
 template <bool COMPACT>
@@ -2242,13 +1934,6 @@ using PathKernel = void (*)(PathArgs);
 
 template <typename T, int BLOCK, bool SMEM>
 PathKernel sssp_kernel(int variant) {
-  if constexpr (std::is_same<T, float>::value) {
-    if (variant == kSsspBucket) return k_sssp_bkt<BLOCK, SMEM, unsigned short>;
-    if (variant == kSsspBucketWide) return k_sssp_bkt<BLOCK, SMEM, unsigned>;
-  } else {  // FP64 labels: the queue kernel (same ring size, same scratch layout)
-    if (variant == kSsspBucket) return k_sssp_nfq<T, BLOCK, SMEM, unsigned short>;
-    if (variant == kSsspBucketWide) return k_sssp_nfq<T, BLOCK, SMEM, unsigned>;
-  }
   if (variant == kSsspRounds) return k_sssp<T, BLOCK, SMEM>;
   if (variant == kSsspAsync) return k_sssp_async<T, BLOCK, SMEM>;
   if (variant == kSsspNearFarQueue) return k_sssp_nfq<T, BLOCK, SMEM, unsigned short>;
@@ -2284,8 +1969,6 @@ size_t sssp_smem_bytes(int n1, bool fp64, int variant) {
   const size_t words = (static_cast<size_t>(n1) + 31) / 32;
   const size_t ring = variant == kSsspNearFarQueue       ? sizeof(unsigned short) * kQCap
                       : variant == kSsspNearFarQueueWide ? sizeof(unsigned) * kQCap
-                      : variant == kSsspBucket           ? sizeof(unsigned short) * kBCap
-                      : variant == kSsspBucketWide       ? sizeof(unsigned) * kBCap
                                                          : 0;
   return align16(align16((fp64 ? 8 : 4) * static_cast<size_t>(n1)) + 2 * 4 * words + ring);
 }
@@ -2309,9 +1992,7 @@ int max_smem_optin(int device) {
 cudaError_t launch_sssp(const PathArgs& a, bool fp64, int grid, int block, bool smem,
                         int variant, cudaStream_t s) {
   // FP32 paths of the queue variant read the padded records
-  if ((variant == kSsspNearFarQueue || variant == kSsspNearFarQueueWide || variant == kSsspBucket ||
-       variant == kSsspBucketWide) &&
-      !fp64 && !a.e4)
+  if ((variant == kSsspNearFarQueue || variant == kSsspNearFarQueueWide) && !fp64 && !a.e4)
     return cudaErrorInvalidValue;
   const size_t bytes = sssp_smem_bytes(a.g.n1, fp64, variant);
 #define TAPGPU_SSSP_CASE(B)                                                              \

@@ -162,9 +162,6 @@ enum : int {
   kSsspNearFar = 3, // asynchronous near set below a rising threshold (k_sssp_nf)
   kSsspNearFarQueue = 4,  // near-far with a FIFO ring of near nodes (k_sssp_nfq)
   kSsspNearFarQueueWide = 5,  // the same with 32-bit ring entries (chosen above 65535 nodes)
-  kSsspBucket = 6,  // near-far in barrier-synchronous rounds, a lane per link (k_sssp_bkt;
-                    // FP32 paths with padded records, at most 65535 nodes)
-  kSsspBucketWide = 7,  // the same with 32-bit ring entries
 };
 constexpr int kQueueSlots = 1024;  // ring slots of k_sssp_nfq
 cudaError_t launch_sssp(const PathArgs& a, bool fp64, int grid, int block, bool smem,

@@ -189,8 +189,7 @@ PathArgs Ctx::path_args(int nscen_slots) const {
   a.scratch_stride = 0;
   a.stats = timing ? path_stats : nullptr;
   a.nf_delta = nf_delta;
-  a.e4 = (!fp64 && (sssp_variant == kSsspNearFarQueue || sssp_variant == kSsspNearFarQueueWide ||
-                    sssp_variant == kSsspBucket || sssp_variant == kSsspBucketWide))
+  a.e4 = (!fp64 && (sssp_variant == kSsspNearFarQueue || sssp_variant == kSsspNearFarQueueWide))
              ? e4
              : nullptr;
   return a;
@@ -324,17 +323,14 @@ int Ctx::plan_launches() {
   num_sms = prop.multiProcessorCount;
   const int optin = max_smem_optin(device);
   ls_mode = opt.line_search == kLsExact ? kLsExact : kLsReference;
-  sssp_variant = (opt.sssp_variant >= kSsspRounds && opt.sssp_variant <= kSsspNearFarQueue) ||
-                         opt.sssp_variant == kSsspBucket
+  sssp_variant = (opt.sssp_variant >= kSsspRounds && opt.sssp_variant <= kSsspNearFarQueue)
                      ? opt.sssp_variant
                      : kSsspNearFarQueue;
-  // the rings of the queue and bucket variants hold 16-bit node ids, and
-  // their padded records 16-bit heads and degrees
+  // the ring of the queue variant holds 16-bit node ids, and its padded
+  // records 16-bit heads and degrees
   if (sssp_variant == kSsspNearFarQueue && !deg16) sssp_variant = kSsspNearFarQueueWide;
-  if (sssp_variant == kSsspBucket && !deg16) sssp_variant = kSsspBucketWide;
   const bool nf = sssp_variant == kSsspNearFar || sssp_variant == kSsspNearFarQueue ||
-                  sssp_variant == kSsspNearFarQueueWide || sssp_variant == kSsspBucket ||
-                  sssp_variant == kSsspBucketWide;
+                  sssp_variant == kSsspNearFarQueueWide;
   sssp_block = opt.sssp_block > 0 ? opt.sssp_block : (nf ? 256 : 512);
   // the ring keeps one free slot per thread
   if ((sssp_variant == kSsspNearFarQueue || sssp_variant == kSsspNearFarQueueWide) &&
