@@ -277,3 +277,49 @@ def test_cli_trip_mods_match_reference_golden(built_lib, tmp_path):
     assert abs(hdr["relgap"] - float(z["hdr_relgap"])) <= 1e-6 * abs(float(z["hdr_relgap"]))
     for col in (1, 2, 4):
         np.testing.assert_allclose(log[:, col], z["log"][:, col], rtol=1e-6)
+
+
+def test_cli_checkpoint_on_sigusr2_and_clean_finish_on_sigterm(built_lib, tmp_path):
+    """SIGUSR2 rewrites the flows file in place with the checkpoint header and
+    the current flows while the solve goes on; SIGTERM then ends it cleanly
+    with the final flows file (tap/tap_frankwolfe_pthread.c:215-254, 766-803).
+    The signals are sent from the host between launches of iterations."""
+    import signal
+    import threading
+    import time
+
+    net, dem = synth.make_grid416()
+    nf, tf = _write_case(net, dem, str(tmp_path))
+    flows = str(tmp_path / "flows.txt")
+    lines = []
+    with open(flows, "w") as out:
+        proc = subprocess.Popen([B.cli_path(), "-n", "1", "-i", "10000000", nf, tf], stdout=out,
+                                stderr=subprocess.PIPE, text=True)
+        reader = threading.Thread(target=lambda: lines.extend(proc.stderr), daemon=True)
+        reader.start()
+        try:
+            time.sleep(3.0)  # past the set-up, inside the iteration loop
+            assert proc.poll() is None, "".join(lines)
+            proc.send_signal(signal.SIGUSR2)
+            t0 = time.time()
+            while not any("checkpointing to flows output file...done" in ln for ln in lines):
+                assert time.time() - t0 < 60, "no checkpoint: " + "".join(lines)[-2000:]
+                time.sleep(0.05)
+            text = open(flows).read()
+            assert text.startswith("~ checkpoint written at ")
+            init, term, vol, cost, hdr = tntp.read_flows(text, is_text=True)
+            assert len(vol) == net.num_links and hdr["iterations"] > 0
+            np.testing.assert_array_equal(init, net.init)
+            assert abs(hdr["totalcost"] - float(vol @ cost)) <= 1e-9 * hdr["totalcost"]
+            # the status line of SIGUSR1 and the checkpoint's both carry the iteration
+            assert any(ln.startswith("iter = ") for ln in lines)
+            proc.send_signal(signal.SIGTERM)
+            rc = proc.wait(timeout=120)
+        finally:
+            if proc.poll() is None:
+                proc.kill()
+                proc.wait()
+    assert rc == 0, "".join(lines)[-2000:]
+    init, term, vol, cost, hdr = tntp.read_flows(flows)
+    assert len(vol) == net.num_links and hdr["iterations"] >= 1
+    assert np.all(vol >= 0) and abs(hdr["totalcost"] - float(vol @ cost)) <= 1e-9 * hdr["totalcost"]
