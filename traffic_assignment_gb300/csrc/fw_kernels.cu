@@ -957,6 +957,86 @@ __device__ __forceinline__ void nfq_expand(const PathArgs& a, const uint2* e4s, 
   if (lane == 0) atomicAdd(pending, -(reserve - used + items));
 }
 
+// Predecessor words of one task from its final FP32 labels (still in shared
+// memory): each node's lowest-numbered tight in-link from a strictly closer
+// tail, the rule k_aon applies (a node's reverse-star slots are in link
+// order, so the first tight slot is that link), packed as (link << 16 |
+// tail) into the task's slot of a.dist in place of the labels; the source
+// and unreachable nodes get kPredRoot.  Nodes reached only over links too
+// short to change their labels (zero or absorbed costs) are attached level
+// by level to already attached nodes of equal label, lowest link first, so
+// the tree stays acyclic, with a per-CTA slice of a.pred_scr as scratch.
+template <int BLOCK>
+__device__ void write_pred_words(const PathArgs& a, const unsigned* dist, int src, int scen,
+                                 int task) {
+  const int n1 = a.g.n1;
+  const int F = a.g.first_thru;
+  unsigned* up = static_cast<unsigned*>(a.dist) + static_cast<size_t>(task - a.task_begin) * n1;
+  const uint2* rr = a.r32 + static_cast<size_t>(scen) * a.g.m;
+  int pend = 0;
+  for (int v = threadIdx.x; v < n1; v += BLOCK) {
+    const unsigned dvb = dist[v];
+    unsigned p = kPredRoot;
+    if (v != src && dvb != DT<float>::kInf) {
+      p = kPredPending;
+      const float dv = __uint_as_float(dvb);
+      const int i1 = __ldg(a.g.in_ptr + v + 1);
+      for (int i = __ldg(a.g.in_ptr + v); i < i1; ++i) {
+        const uint2 r = __ldg(rr + i);
+        const int u = static_cast<int>(r.x);
+        if (u < F && u != src) continue;  // zones are never passed through
+        const float du = __uint_as_float(dist[u]);
+        if (du < dv && __fadd_rn(du, __uint_as_float(r.y)) == dv) {
+          p = (static_cast<unsigned>(__ldg(a.g.in_link + i)) << 16) | static_cast<unsigned>(u);
+          break;
+        }
+      }
+      pend |= p == kPredPending ? 1 : 0;
+    }
+    up[v] = p;
+  }
+  if (!__syncthreads_or(pend)) return;
+  unsigned* scr = a.pred_scr + static_cast<size_t>(blockIdx.x) * n1;
+  for (int guard = 0;;) {
+    for (int v = threadIdx.x; v < n1; v += BLOCK) {
+      if (up[v] != kPredPending) continue;
+      unsigned c = kPredPending;
+      const float dv = __uint_as_float(dist[v]);
+      const int i1 = __ldg(a.g.in_ptr + v + 1);
+      for (int i = __ldg(a.g.in_ptr + v); i < i1; ++i) {
+        const uint2 r = __ldg(rr + i);
+        const int u = static_cast<int>(r.x);
+        if (u < F && u != src) continue;
+        if (!(u == src || up[u] < kPredRoot)) continue;
+        if (__fadd_rn(__uint_as_float(dist[u]), __uint_as_float(r.y)) == dv) {
+          c = (static_cast<unsigned>(__ldg(a.g.in_link + i)) << 16) | static_cast<unsigned>(u);
+          break;
+        }
+      }
+      scr[v] = c;
+    }
+    __syncthreads();
+    int progress = 0, still = 0;
+    for (int v = threadIdx.x; v < n1; v += BLOCK) {
+      if (up[v] != kPredPending) continue;
+      const unsigned c = scr[v];
+      if (c != kPredPending) {
+        up[v] = c;
+        progress = 1;
+      } else {
+        still = 1;
+      }
+    }
+    const int any_progress = __syncthreads_or(progress);
+    const int any_still = __syncthreads_or(still);
+    if (!any_still) break;
+    if (!any_progress || ++guard > n1) {
+      if (threadIdx.x == 0) atomicOr(a.err, kErrPending);
+      break;
+    }
+  }
+}
+
 // five 256-thread CTAs per SM fit the shared memory of a 10k-node network:
 // keep registers to that occupancy
 template <typename T, int BLOCK, bool SMEM, typename R>
@@ -1202,8 +1282,17 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
         break;
       }
     }
-    T* out = static_cast<T*>(a.dist) + static_cast<size_t>(task - a.task_begin) * n1;
-    for (int v = threadIdx.x; v < n1; v += BLOCK) out[v] = DT<T>::val(dist[v]);
+    bool trees = false;  // (uniform: a launch argument)
+    if constexpr (std::is_same<T, float>::value && std::is_same<R, unsigned short>::value) {
+      if (a.pred_words) {
+        write_pred_words<BLOCK>(a, dist, src, scen, task);
+        trees = true;
+      }
+    }
+    if (!trees) {
+      T* out = static_cast<T*>(a.dist) + static_cast<size_t>(task - a.task_begin) * n1;
+      for (int v = threadIdx.x; v < n1; v += BLOCK) out[v] = DT<T>::val(dist[v]);
+    }
     if (a.stats) {
       for (int o = 16; o >= 1; o >>= 1) expanded += __shfl_down_sync(kFull, expanded, o);
       if (lane == 0) {
@@ -1275,6 +1364,24 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
     int* gslot = reinterpret_cast<int*>(const_cast<T*>(din));
     int* scr = COMPACT ? gslot : parent;
 
+    // predecessor words from the path kernel (compact layout): no labels, no sweep
+    const bool given = COMPACT && a.pred_words;  // (uniform: a launch argument)
+    unsigned* up = reinterpret_cast<unsigned*>(pred);
+    if (given) {
+      const unsigned* pin = reinterpret_cast<const unsigned*>(din);
+      int v = threadIdx.x;
+      for (; v + 3 * BLOCK < n1; v += 4 * BLOCK) {
+        const unsigned p0 = pin[v], p1 = pin[v + BLOCK], p2 = pin[v + 2 * BLOCK], p3 = pin[v + 3 * BLOCK];
+        up[v] = p0;
+        up[v + BLOCK] = p1;
+        up[v + 2 * BLOCK] = p2;
+        up[v + 3 * BLOCK] = p3;
+      }
+      for (; v < n1; v += BLOCK) up[v] = pin[v];
+      __syncthreads();
+    }
+    const bool pack = COMPACT && a.g.m <= 0xffff;
+    if (!given) {
     // labels in, several loads in flight per thread; predecessors cleared
     {
       int v = threadIdx.x;
@@ -1290,8 +1397,6 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
     // Predecessor words: the link id, or (link << 16 | tail) when links and
     // nodes both fit 16 bits (the compact layout), so that the parents need
     // no lookup of the link's tail; the minimum still orders by link.
-    const bool pack = COMPACT && a.g.m <= 0xffff;
-    unsigned* up = reinterpret_cast<unsigned*>(pred);
     for (int v = threadIdx.x; v < n1; v += BLOCK) up[v] = kPredNone;
     __syncthreads();
 
@@ -1381,6 +1486,7 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
         break;
       }
     }
+    }  // (!given)
     __syncthreads();  // (COMPACT: the scratch reads of the loop above precede the links' writes)
     for (int v = threadIdx.x; v < n1; v += BLOCK) {
       const unsigned p = up[v];
