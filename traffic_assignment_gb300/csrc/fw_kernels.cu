@@ -966,34 +966,77 @@ __device__ __forceinline__ void nfq_expand(const PathArgs& a, const uint2* e4s, 
 // short to change their labels (zero or absorbed costs) are attached level
 // by level to already attached nodes of equal label, lowest link first, so
 // the tree stays acyclic, with a per-CTA slice of a.pred_scr as scratch.
+// (out of line: it runs once per task, and its registers stay apart from
+// the relaxation loop's)
 template <int BLOCK>
-__device__ void write_pred_words(const PathArgs& a, const unsigned* dist, int src, int scen,
-                                 int task) {
+__device__ __noinline__ void write_pred_words(const PathArgs& a, const unsigned* dist, int src,
+                                              int scen, int task) {
   const int n1 = a.g.n1;
   const int F = a.g.first_thru;
   unsigned* up = static_cast<unsigned*>(a.dist) + static_cast<size_t>(task - a.task_begin) * n1;
   const uint2* rr = a.r32 + static_cast<size_t>(scen) * a.g.m;
+  // Four nodes per thread at a time, their in-links scanned in step (the
+  // k-th in-link of each in one pass), so that four chains of global loads
+  // are in flight together; the link id of the chosen slot is read last.
+  constexpr int kNodes = 4;
   int pend = 0;
-  for (int v = threadIdx.x; v < n1; v += BLOCK) {
-    const unsigned dvb = dist[v];
-    unsigned p = kPredRoot;
-    if (v != src && dvb != DT<float>::kInf) {
-      p = kPredPending;
-      const float dv = __uint_as_float(dvb);
-      const int i1 = __ldg(a.g.in_ptr + v + 1);
-      for (int i = __ldg(a.g.in_ptr + v); i < i1; ++i) {
-        const uint2 r = __ldg(rr + i);
-        const int u = static_cast<int>(r.x);
-        if (u < F && u != src) continue;  // zones are never passed through
-        const float du = __uint_as_float(dist[u]);
-        if (du < dv && __fadd_rn(du, __uint_as_float(r.y)) == dv) {
-          p = (static_cast<unsigned>(__ldg(a.g.in_link + i)) << 16) | static_cast<unsigned>(u);
-          break;
+  for (int v0 = threadIdx.x; v0 < n1; v0 += kNodes * BLOCK) {
+    int ia[kNodes], ib[kNodes], bi[kNodes], bu[kNodes];
+    float dv[kNodes];
+#pragma unroll
+    for (int j = 0; j < kNodes; ++j) {
+      const int v = v0 + j * BLOCK;
+      ia[j] = ib[j] = 0;
+      bi[j] = -1;  // slot of the chosen in-link
+      bu[j] = 0;
+      dv[j] = 0.f;
+      if (v < n1) {
+        const unsigned dvb = dist[v];
+        if (v != src && dvb != DT<float>::kInf) {
+          dv[j] = __uint_as_float(dvb);
+          ia[j] = __ldg(a.g.in_ptr + v);
+          ib[j] = __ldg(a.g.in_ptr + v + 1);
         }
       }
-      pend |= p == kPredPending ? 1 : 0;
     }
-    up[v] = p;
+    for (int k = 0;; ++k) {
+      bool any = false;
+#pragma unroll
+      for (int j = 0; j < kNodes; ++j) {
+        const int i = ia[j] + k;
+        if (bi[j] < 0 && i < ib[j]) {
+          any = true;
+          const uint2 r = __ldg(rr + i);
+          const int u = static_cast<int>(r.x);
+          if (!(u < F && u != src)) {  // zones are never passed through
+            const float du = __uint_as_float(dist[u]);
+            if (du < dv[j] && __fadd_rn(du, __uint_as_float(r.y)) == dv[j]) {
+              bi[j] = i;
+              bu[j] = u;
+            }
+          }
+        }
+      }
+      if (!any) break;
+    }
+    unsigned lk[kNodes];
+#pragma unroll
+    for (int j = 0; j < kNodes; ++j) lk[j] = bi[j] >= 0 ? __ldg(a.g.in_link + bi[j]) : 0u;
+#pragma unroll
+    for (int j = 0; j < kNodes; ++j) {
+      const int v = v0 + j * BLOCK;
+      if (v >= n1) continue;
+      unsigned p = kPredRoot;  // the source, or unreachable
+      if (v != src && dist[v] != DT<float>::kInf) {
+        if (bi[j] >= 0) {
+          p = (lk[j] << 16) | static_cast<unsigned>(bu[j]);
+        } else {
+          p = kPredPending;
+          pend = 1;
+        }
+      }
+      up[v] = p;
+    }
   }
   if (!__syncthreads_or(pend)) return;
   unsigned* scr = a.pred_scr + static_cast<size_t>(blockIdx.x) * n1;
