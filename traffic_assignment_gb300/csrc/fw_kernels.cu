@@ -966,11 +966,9 @@ __device__ __forceinline__ void nfq_expand(const PathArgs& a, const uint2* e4s, 
 // short to change their labels (zero or absorbed costs) are attached level
 // by level to already attached nodes of equal label, lowest link first, so
 // the tree stays acyclic, with a per-CTA slice of a.pred_scr as scratch.
-// (out of line: it runs once per task, and its registers stay apart from
-// the relaxation loop's)
 template <int BLOCK>
-__device__ __noinline__ void write_pred_words(const PathArgs& a, const unsigned* dist, int src,
-                                              int scen, int task) {
+__device__ __forceinline__ void write_pred_words(const PathArgs& a, const unsigned* dist, int src,
+                                                 int scen, int task) {
   const int n1 = a.g.n1;
   const int F = a.g.first_thru;
   unsigned* up = static_cast<unsigned*>(a.dist) + static_cast<size_t>(task - a.task_begin) * n1;
@@ -978,7 +976,7 @@ __device__ __noinline__ void write_pred_words(const PathArgs& a, const unsigned*
   // Four nodes per thread at a time, their in-links scanned in step (the
   // k-th in-link of each in one pass), so that four chains of global loads
   // are in flight together; the link id of the chosen slot is read last.
-  constexpr int kNodes = 4;
+  constexpr int kNodes = 2;
   int pend = 0;
   for (int v0 = threadIdx.x; v0 < n1; v0 += kNodes * BLOCK) {
     int ia[kNodes], ib[kNodes], bi[kNodes], bu[kNodes];
@@ -1082,7 +1080,10 @@ __device__ __noinline__ void write_pred_words(const PathArgs& a, const unsigned*
 
 // five 256-thread CTAs per SM fit the shared memory of a 10k-node network:
 // keep registers to that occupancy
-template <typename T, int BLOCK, bool SMEM, typename R>
+// TREES (FP32 labels, 16-bit nodes): the task ends with write_pred_words
+// instead of writing its labels (a separate instantiation, so that the
+// label-writing kernel is unchanged)
+template <typename T, int BLOCK, bool SMEM, typename R, bool TREES = false>
 __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) k_sssp_nfq(PathArgs a) {
   using U = typename DT<T>::U;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1325,14 +1326,11 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
         break;
       }
     }
-    bool trees = false;  // (uniform: a launch argument)
-    if constexpr (std::is_same<T, float>::value && std::is_same<R, unsigned short>::value) {
-      if (a.pred_words) {
-        write_pred_words<BLOCK>(a, dist, src, scen, task);
-        trees = true;
-      }
-    }
-    if (!trees) {
+    if constexpr (TREES) {
+      static_assert(std::is_same<T, float>::value && std::is_same<R, unsigned short>::value,
+                    "predecessor words pack 16-bit links and nodes from FP32 labels");
+      write_pred_words<BLOCK>(a, dist, src, scen, task);
+    } else {
       T* out = static_cast<T*>(a.dist) + static_cast<size_t>(task - a.task_begin) * n1;
       for (int v = threadIdx.x; v < n1; v += BLOCK) out[v] = DT<T>::val(dist[v]);
     }
@@ -2093,6 +2091,10 @@ PathKernel sssp_kernel(int variant) {
 template <typename T, int BLOCK, bool SMEM>
 cudaError_t launch_sssp_t(const PathArgs& a, int grid, size_t smem, int variant, cudaStream_t s) {
   PathKernel fn = sssp_kernel<T, BLOCK, SMEM>(variant);
+  if constexpr (std::is_same<T, float>::value) {
+    if (a.pred_words && variant == kSsspNearFarQueue)
+      fn = k_sssp_nfq<float, BLOCK, SMEM, unsigned short, true>;
+  }
   if (SMEM) {
     cudaError_t e = allow_max_smem(fn);
     if (e != cudaSuccess) return e;
