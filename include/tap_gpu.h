@@ -246,11 +246,6 @@ typedef struct tapgpu_options_s {
                             derivative (differentiable step sizes, for the adjoint) */
   int tape_checkpoint;   /* with record_tape: flows kept every this many iterations and
                             recomputed in between by the adjoint (0 = sqrt(tape_capacity)) */
-  int separate_trees;    /* FP32 path costs on networks of at most 65535 nodes and links:
-                            0 (default) the shortest-path kernel also picks each node's
-                            predecessor while the labels are on chip and hands the loading
-                            kernel predecessor words instead of labels; 1 the loading kernel
-                            rebuilds the trees from the labels (same trees, same flows) */
 } tapgpu_options;
 
 typedef struct tapgpu_result_s {

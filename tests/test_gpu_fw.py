@@ -309,46 +309,3 @@ def test_queue_kernel_equals_near_far_kernel(built_lib, case):
     np.testing.assert_array_equal(outs["nearfar_queue"][0], outs["nearfar"][0])
     np.testing.assert_array_equal(outs["nearfar_queue"][1], outs["nearfar"][1])
     assert outs["nearfar_queue"][2] == outs["nearfar"][2]
-
-
-@pytest.mark.parametrize("case", ["grid416", "grid3600_global", "grid10k_batch", "zero_costs",
-                                  "centroids"])
-def test_trees_from_path_kernel_equal_loading_kernel_trees(built_lib, case):
-    """FP32 paths on compact networks: the predecessor words the path kernel
-    picks while its labels are on chip give the same trees, bit-identical
-    flows and the same gaps as the loading kernel rebuilding the trees from
-    the labels: single scenarios, labels in global memory, a batch of
-    warm-started scenarios, links of zero free-flow time (nodes reached only
-    over them need the level-by-level attachment), zone-only nodes."""
-    kw = {}
-    if case == "grid3600_global":
-        net, dem = synth.make_grid3600()
-        kw["global_scratch"] = True
-    elif case == "grid10k_batch":
-        net, dem = synth.make_grid10k()
-    elif case == "centroids":
-        net, dem = synth.make_grid416_centroids()
-    else:
-        net, dem = synth.make_grid416()
-    if case == "zero_costs":
-        net = net.copy()
-        rng = np.random.default_rng(3)
-        net.fft[rng.choice(net.num_links, 60, replace=False)] = 0.0
-    outs = {}
-    for separate in (True, False):
-        with Solver(net, dem, precision="fp32", separate_trees=separate, **kw) as s:
-            if case == "grid10k_batch":
-                s.solve(max_iters=6)
-                x0, _ = s.flows()
-                scen = synth.make_scenarios(net, 12)
-                res = s.solve_scenarios(scen, max_iters=5, x0=x0)
-                x, t = s.flows_batch(0, len(scen))
-                outs[separate] = (x, t, [q["relgap"] for q in res], [q["error_bits"] for q in res])
-            else:
-                r = s.solve(max_iters=15)
-                x, t = s.flows()
-                outs[separate] = (x, t, [r["relgap"]], [r["error_bits"]])
-    np.testing.assert_array_equal(outs[False][0], outs[True][0])
-    np.testing.assert_array_equal(outs[False][1], outs[True][1])
-    assert outs[False][2] == outs[True][2]
-    assert outs[False][3] == outs[True][3] and all(e == 0 for e in outs[True][3])

@@ -957,133 +957,9 @@ __device__ __forceinline__ void nfq_expand(const PathArgs& a, const uint2* e4s, 
   if (lane == 0) atomicAdd(pending, -(reserve - used + items));
 }
 
-// Predecessor words of one task from its final FP32 labels (still in shared
-// memory): each node's lowest-numbered tight in-link from a strictly closer
-// tail, the rule k_aon applies (a node's reverse-star slots are in link
-// order, so the first tight slot is that link), packed as (link << 16 |
-// tail) into the task's slot of a.dist in place of the labels; the source
-// and unreachable nodes get kPredRoot.  Nodes reached only over links too
-// short to change their labels (zero or absorbed costs) are attached level
-// by level to already attached nodes of equal label, lowest link first, so
-// the tree stays acyclic, with a per-CTA slice of a.pred_scr as scratch.
-template <int BLOCK>
-__device__ __forceinline__ void write_pred_words(const PathArgs& a, const unsigned* dist, int src,
-                                                 int scen, int task) {
-  const int n1 = a.g.n1;
-  const int F = a.g.first_thru;
-  unsigned* up = static_cast<unsigned*>(a.dist) + static_cast<size_t>(task - a.task_begin) * n1;
-  const uint2* rr = a.r32 + static_cast<size_t>(scen) * a.g.m;
-  // Four nodes per thread at a time, their in-links scanned in step (the
-  // k-th in-link of each in one pass), so that four chains of global loads
-  // are in flight together; the link id of the chosen slot is read last.
-  constexpr int kNodes = 2;
-  int pend = 0;
-  for (int v0 = threadIdx.x; v0 < n1; v0 += kNodes * BLOCK) {
-    int ia[kNodes], ib[kNodes], bi[kNodes], bu[kNodes];
-    float dv[kNodes];
-#pragma unroll
-    for (int j = 0; j < kNodes; ++j) {
-      const int v = v0 + j * BLOCK;
-      ia[j] = ib[j] = 0;
-      bi[j] = -1;  // slot of the chosen in-link
-      bu[j] = 0;
-      dv[j] = 0.f;
-      if (v < n1) {
-        const unsigned dvb = dist[v];
-        if (v != src && dvb != DT<float>::kInf) {
-          dv[j] = __uint_as_float(dvb);
-          ia[j] = __ldg(a.g.in_ptr + v);
-          ib[j] = __ldg(a.g.in_ptr + v + 1);
-        }
-      }
-    }
-    for (int k = 0;; ++k) {
-      bool any = false;
-#pragma unroll
-      for (int j = 0; j < kNodes; ++j) {
-        const int i = ia[j] + k;
-        if (bi[j] < 0 && i < ib[j]) {
-          any = true;
-          const uint2 r = __ldg(rr + i);
-          const int u = static_cast<int>(r.x);
-          if (!(u < F && u != src)) {  // zones are never passed through
-            const float du = __uint_as_float(dist[u]);
-            if (du < dv[j] && __fadd_rn(du, __uint_as_float(r.y)) == dv[j]) {
-              bi[j] = i;
-              bu[j] = u;
-            }
-          }
-        }
-      }
-      if (!any) break;
-    }
-    unsigned lk[kNodes];
-#pragma unroll
-    for (int j = 0; j < kNodes; ++j) lk[j] = bi[j] >= 0 ? __ldg(a.g.in_link + bi[j]) : 0u;
-#pragma unroll
-    for (int j = 0; j < kNodes; ++j) {
-      const int v = v0 + j * BLOCK;
-      if (v >= n1) continue;
-      unsigned p = kPredRoot;  // the source, or unreachable
-      if (v != src && dist[v] != DT<float>::kInf) {
-        if (bi[j] >= 0) {
-          p = (lk[j] << 16) | static_cast<unsigned>(bu[j]);
-        } else {
-          p = kPredPending;
-          pend = 1;
-        }
-      }
-      up[v] = p;
-    }
-  }
-  if (!__syncthreads_or(pend)) return;
-  unsigned* scr = a.pred_scr + static_cast<size_t>(blockIdx.x) * n1;
-  for (int guard = 0;;) {
-    for (int v = threadIdx.x; v < n1; v += BLOCK) {
-      if (up[v] != kPredPending) continue;
-      unsigned c = kPredPending;
-      const float dv = __uint_as_float(dist[v]);
-      const int i1 = __ldg(a.g.in_ptr + v + 1);
-      for (int i = __ldg(a.g.in_ptr + v); i < i1; ++i) {
-        const uint2 r = __ldg(rr + i);
-        const int u = static_cast<int>(r.x);
-        if (u < F && u != src) continue;
-        if (!(u == src || up[u] < kPredRoot)) continue;
-        if (__fadd_rn(__uint_as_float(dist[u]), __uint_as_float(r.y)) == dv) {
-          c = (static_cast<unsigned>(__ldg(a.g.in_link + i)) << 16) | static_cast<unsigned>(u);
-          break;
-        }
-      }
-      scr[v] = c;
-    }
-    __syncthreads();
-    int progress = 0, still = 0;
-    for (int v = threadIdx.x; v < n1; v += BLOCK) {
-      if (up[v] != kPredPending) continue;
-      const unsigned c = scr[v];
-      if (c != kPredPending) {
-        up[v] = c;
-        progress = 1;
-      } else {
-        still = 1;
-      }
-    }
-    const int any_progress = __syncthreads_or(progress);
-    const int any_still = __syncthreads_or(still);
-    if (!any_still) break;
-    if (!any_progress || ++guard > n1) {
-      if (threadIdx.x == 0) atomicOr(a.err, kErrPending);
-      break;
-    }
-  }
-}
-
 // five 256-thread CTAs per SM fit the shared memory of a 10k-node network:
 // keep registers to that occupancy
-// TREES (FP32 labels, 16-bit nodes): the task ends with write_pred_words
-// instead of writing its labels (a separate instantiation, so that the
-// label-writing kernel is unchanged)
-template <typename T, int BLOCK, bool SMEM, typename R, bool TREES = false>
+template <typename T, int BLOCK, bool SMEM, typename R>
 __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) k_sssp_nfq(PathArgs a) {
   using U = typename DT<T>::U;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1326,14 +1202,8 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
         break;
       }
     }
-    if constexpr (TREES) {
-      static_assert(std::is_same<T, float>::value && std::is_same<R, unsigned short>::value,
-                    "predecessor words pack 16-bit links and nodes from FP32 labels");
-      write_pred_words<BLOCK>(a, dist, src, scen, task);
-    } else {
-      T* out = static_cast<T*>(a.dist) + static_cast<size_t>(task - a.task_begin) * n1;
-      for (int v = threadIdx.x; v < n1; v += BLOCK) out[v] = DT<T>::val(dist[v]);
-    }
+    T* out = static_cast<T*>(a.dist) + static_cast<size_t>(task - a.task_begin) * n1;
+    for (int v = threadIdx.x; v < n1; v += BLOCK) out[v] = DT<T>::val(dist[v]);
     if (a.stats) {
       for (int o = 16; o >= 1; o >>= 1) expanded += __shfl_down_sync(kFull, expanded, o);
       if (lane == 0) {
@@ -1405,24 +1275,6 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
     int* gslot = reinterpret_cast<int*>(const_cast<T*>(din));
     int* scr = COMPACT ? gslot : parent;
 
-    // predecessor words from the path kernel (compact layout): no labels, no sweep
-    const bool given = COMPACT && a.pred_words;  // (uniform: a launch argument)
-    unsigned* up = reinterpret_cast<unsigned*>(pred);
-    if (given) {
-      const unsigned* pin = reinterpret_cast<const unsigned*>(din);
-      int v = threadIdx.x;
-      for (; v + 3 * BLOCK < n1; v += 4 * BLOCK) {
-        const unsigned p0 = pin[v], p1 = pin[v + BLOCK], p2 = pin[v + 2 * BLOCK], p3 = pin[v + 3 * BLOCK];
-        up[v] = p0;
-        up[v + BLOCK] = p1;
-        up[v + 2 * BLOCK] = p2;
-        up[v + 3 * BLOCK] = p3;
-      }
-      for (; v < n1; v += BLOCK) up[v] = pin[v];
-      __syncthreads();
-    }
-    const bool pack = COMPACT && a.g.m <= 0xffff;
-    if (!given) {
     // labels in, several loads in flight per thread; predecessors cleared
     {
       int v = threadIdx.x;
@@ -1438,6 +1290,8 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
     // Predecessor words: the link id, or (link << 16 | tail) when links and
     // nodes both fit 16 bits (the compact layout), so that the parents need
     // no lookup of the link's tail; the minimum still orders by link.
+    const bool pack = COMPACT && a.g.m <= 0xffff;
+    unsigned* up = reinterpret_cast<unsigned*>(pred);
     for (int v = threadIdx.x; v < n1; v += BLOCK) up[v] = kPredNone;
     __syncthreads();
 
@@ -1527,7 +1381,6 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
         break;
       }
     }
-    }  // (!given)
     __syncthreads();  // (COMPACT: the scratch reads of the loop above precede the links' writes)
     for (int v = threadIdx.x; v < n1; v += BLOCK) {
       const unsigned p = up[v];
@@ -2091,10 +1944,6 @@ PathKernel sssp_kernel(int variant) {
 template <typename T, int BLOCK, bool SMEM>
 cudaError_t launch_sssp_t(const PathArgs& a, int grid, size_t smem, int variant, cudaStream_t s) {
   PathKernel fn = sssp_kernel<T, BLOCK, SMEM>(variant);
-  if constexpr (std::is_same<T, float>::value) {
-    if (a.pred_words && variant == kSsspNearFarQueue)
-      fn = k_sssp_nfq<float, BLOCK, SMEM, unsigned short, true>;
-  }
   if (SMEM) {
     cudaError_t e = allow_max_smem(fn);
     if (e != cudaSuccess) return e;

@@ -101,10 +101,6 @@ struct PathArgs {
   unsigned long long* y_fx;     // [S][m]
   int* pred_out;                // [(t - task_begin)][n1] predecessor links, optional
   int do_load;                  // 0: predecessors only
-  int pred_words;               // FP32 paths, compact trees: the path kernel writes each
-                                // task's predecessor words (link << 16 | tail) into its
-                                // slot of `dist` instead of labels; k_aon reads them
-  unsigned* pred_scr;           // [grid][n1] per-CTA scratch of the rare zero-cost attachment
   void* scratch;                // per-CTA global scratch when the smem variant does not fit
   long long scratch_stride;     // bytes per CTA
   unsigned long long* stats;    // optional [4]: rounds, tasks, node expansions, -

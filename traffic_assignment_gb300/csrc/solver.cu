@@ -192,8 +192,6 @@ PathArgs Ctx::path_args(int nscen_slots) const {
   a.e4 = (!fp64 && (sssp_variant == kSsspNearFarQueue || sssp_variant == kSsspNearFarQueueWide))
              ? e4
              : nullptr;
-  a.pred_words = pred_words ? 1 : 0;
-  a.pred_scr = pred_scr;
   return a;
 }
 
@@ -359,13 +357,6 @@ int Ctx::plan_launches() {
     path_scratch_bytes = scratch;
   }
   link_grid = std::max(1, std::min((M + 255) / 256, 2 * num_sms));
-  // FP32 paths on the queue kernel with compact trees (nodes and links in
-  // 16 bits): the path kernel picks the predecessors while its labels are on
-  // chip and the loading kernel never reads labels
-  pred_words = !fp64 && !opt.separate_trees && sssp_variant == kSsspNearFarQueue &&
-               aon_compact(n1, false) && M <= 0xffff;
-  if (pred_words)
-    TG_TRY(alloc_n(&pred_scr, static_cast<size_t>(sssp_grid) * static_cast<size_t>(n1)));
   return TAPGPU_OK;
 }
 

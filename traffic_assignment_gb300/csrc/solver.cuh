@@ -112,11 +112,6 @@ struct Ctx {
   int* err = nullptr;       // [1]
   int* err_info = nullptr;  // [2]
   int* pred_buf = nullptr;  // [dist_tasks][n1] for the shortest-path API
-  // the path kernel hands the loading kernel predecessor words instead of
-  // labels (FP32 paths, queue kernel, compact trees); per-CTA scratch for
-  // its rare zero-cost attachment
-  bool pred_words = false;
-  unsigned* pred_scr = nullptr;
   unsigned long long* path_stats = nullptr;  // [8] rounds, tasks, expansions, idle polls, batches
   // buffers of the one-shot API (weights in both precisions, loaded volumes)
   uint2* api_e32 = nullptr;

@@ -59,7 +59,7 @@ class Solver:
                  record_tape: bool = False, tape_capacity: int = 0,
                  global_scratch: bool = False, sssp_variant: str = "default",
                  nf_delta: float = 0.0, line_search: str = "reference",
-                 tape_checkpoint: int = 0, separate_trees: bool = False):
+                 tape_checkpoint: int = 0):
         self.L = K.load()
         self.net = net
         self.dem = dem
@@ -80,7 +80,6 @@ class Solver:
         opt.nf_delta = float(nf_delta)
         opt.line_search = {"reference": 0, "exact": 1}[line_search]
         opt.tape_checkpoint = int(tape_checkpoint)
-        opt.separate_trees = 1 if separate_trees else 0
         self.precision = "fp32" if opt.precision == K.TAPGPU_FP32_PATHS else "fp64"
         self.last_scenarios = 1
         keep: list = []
