@@ -239,8 +239,7 @@ typedef struct tapgpu_options_s {
   int sssp_variant;      /* 0 default (4, or 3 above 65535 nodes); 1 bulk-synchronous
                             rounds; 2 asynchronous warp-owned frontier; 3 asynchronous near
                             set below a rising threshold; 4 as 3 with a FIFO ring of near
-                            nodes (networks of at most 65535 nodes); 6 as 4 on two
-                            scenarios of one origin at once (FP32 path costs; FP64 runs 4) */
+                            nodes (networks of at most 65535 nodes) */
   double nf_delta;       /* threshold step of variants 3 and 4 in cost units; 0 = 16 x mean
                             link cost */
   int line_search;       /* 0: the reference's 2^-k rule; 1: exact root of the directional

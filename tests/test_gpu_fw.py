@@ -309,55 +309,3 @@ def test_queue_kernel_equals_near_far_kernel(built_lib, case):
     np.testing.assert_array_equal(outs["nearfar_queue"][0], outs["nearfar"][0])
     np.testing.assert_array_equal(outs["nearfar_queue"][1], outs["nearfar"][1])
     assert outs["nearfar_queue"][2] == outs["nearfar"][2]
-
-
-@pytest.mark.parametrize("case", ["grid416_single", "grid3600_global", "grid10k_batch12",
-                                  "grid10k_batch13_chunked", "centroids_batch5",
-                                  "grid416_wide_delta", "fp64_falls_back"])
-def test_pair_kernel_equals_queue_kernel(built_lib, case):
-    """Two scenarios of one origin in one CTA (shared frontier, both label
-    sets) reach each scenario's own least fixed point: labels, trees and
-    flows bit-identical to the one-scenario queue kernel.  A lone scenario
-    pairs with itself; odd batches end on a lone slot; chunks of the label
-    buffer hold whole pairs; labels in global memory; zone-only nodes; one
-    near set for the whole graph (the ring overflows into the bitmap); FP64
-    labels run the queue kernel."""
-    kw, prec, nscen = {}, "fp32", 0
-    if case == "grid3600_global":
-        net, dem = synth.make_grid3600()
-        kw["global_scratch"] = True
-        nscen = 4
-    elif case.startswith("grid10k"):
-        net, dem = synth.make_grid10k()
-        nscen = 13 if "13" in case else 12
-        if "chunked" in case:
-            kw["chunk_tasks"] = 2 * net.num_zones + 777  # whole pairs: two slots per chunk
-    elif case == "centroids_batch5":
-        net, dem = synth.make_grid416_centroids()
-        nscen = 5
-    else:
-        net, dem = synth.make_grid416()
-    if case == "grid416_wide_delta":
-        kw["nf_delta"] = 1e9
-        nscen = 3
-    if case == "fp64_falls_back":
-        prec = "fp64"
-        nscen = 3
-    outs = {}
-    for variant in ("nearfar_queue", "nearfar_queue_pair"):
-        with Solver(net, dem, precision=prec, sssp_variant=variant, **kw) as s:
-            if nscen:
-                s.solve(max_iters=5)
-                x0, _ = s.flows()
-                scen = synth.make_scenarios(net, nscen)
-                res = s.solve_scenarios(scen, max_iters=5, x0=x0)
-                x, t = s.flows_batch(0, len(scen))
-                outs[variant] = (x, t, [(q["relgap"], q["error_bits"]) for q in res])
-            else:
-                r = s.solve(max_iters=15)
-                x, t = s.flows()
-                outs[variant] = (x, t, [(r["relgap"], r["error_bits"])])
-    np.testing.assert_array_equal(outs["nearfar_queue_pair"][0], outs["nearfar_queue"][0])
-    np.testing.assert_array_equal(outs["nearfar_queue_pair"][1], outs["nearfar_queue"][1])
-    assert outs["nearfar_queue_pair"][2] == outs["nearfar_queue"][2]
-    assert all(e == 0 for _, e in outs["nearfar_queue"][2])

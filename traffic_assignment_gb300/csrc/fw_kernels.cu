@@ -1220,386 +1220,6 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
   }
 }
 
-// ---------------------------------------------------------------------------
-// k_sssp_nfq2: the queue kernel for two scenarios of one origin at once
-// ---------------------------------------------------------------------------
-// Two upgrade scenarios of a batch share the graph and nearly all link costs,
-// so their label-correcting runs from one origin touch nearly the same nodes
-// in nearly the same order.  k_sssp_nfq2 runs them together in one CTA: each
-// node holds both labels (8 bytes), and one near/far membership, ring entry,
-// claim, degree read and pending reservation serve both; expanding a node
-// relaxes its links for both scenarios (each link's two weights from the two
-// scenarios' padded records).  A node joins the near set when either of its
-// labels drops below the threshold and the far set when either drops at or
-// above it; an expansion propagates both current labels, so every
-// improvement in either scenario is propagated after it happens and both
-// label sets reach their own least fixed point: the labels equal
-// k_sssp_nfq's bit for bit.  FP32 paths, 16-bit nodes.  A task is (pair of
-// scenario slots 2p, 2p+1 of the launch's slots, origin); a lone last slot
-// is run paired with itself and written once.
-template <int BLOCK>
-__device__ __forceinline__ void nfq2_expand(const PathArgs& a, const uint2* e4a, const uint2* e4b,
-                                            const uint2* csra, const uint2* csrb, int src,
-                                            int F, unsigned* dist, unsigned* near,
-                                            unsigned* far, unsigned thr,
-                                            unsigned short* ring, unsigned* qhead,
-                                            unsigned* qtail, int* pending, int* ovf, int v,
-                                            bool valid, unsigned& expanded) {
-  const int lane = threadIdx.x & 31;
-  const bool expand = valid && !(v < F && v != src);
-  int deg = 0;
-  uint2 r4[4];
-  unsigned wb[4];
-  if (expand) {
-    const uint4* pa = reinterpret_cast<const uint4*>(e4a + static_cast<size_t>(v) * 4);
-    const uint4* pb = reinterpret_cast<const uint4*>(e4b + static_cast<size_t>(v) * 4);
-    const uint4 qa0 = __ldg(pa), qa1 = __ldg(pa + 1), qb0 = __ldg(pb), qb1 = __ldg(pb + 1);
-    deg = static_cast<int>(qa0.x >> 16);
-    r4[0] = make_uint2(qa0.x & 0xffffu, qa0.y);
-    r4[1] = make_uint2(qa0.z & 0xffffu, qa0.w);
-    r4[2] = make_uint2(qa1.x & 0xffffu, qa1.y);
-    r4[3] = make_uint2(qa1.z & 0xffffu, qa1.w);
-    wb[0] = qb0.y;
-    wb[1] = qb0.w;
-    wb[2] = qb1.y;
-    wb[3] = qb1.w;
-  }
-  const int packed = warp_sum((deg << 6) | (valid ? 1 : 0));
-  const int reserve = packed >> 6, items = packed & 63;
-  if (lane == 0) atomicAdd(pending, reserve);
-  __syncwarp();
-  int pushes = 0;
-  if (deg > 0) {
-    const unsigned long long d2 = vload(reinterpret_cast<unsigned long long*>(dist) + v);
-    const float dua = __uint_as_float(static_cast<unsigned>(d2));
-    const float dub = __uint_as_float(static_cast<unsigned>(d2 >> 32));
-    for (int base = 0;;) {
-      unsigned pm = 0u;
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        if (base + j >= deg) break;
-        const int h = static_cast<int>(r4[j].x);
-        const unsigned nba = __float_as_uint(__fadd_rn(dua, __uint_as_float(r4[j].y)));
-        const unsigned nbb = __float_as_uint(__fadd_rn(dub, __uint_as_float(wb[j])));
-        const unsigned olda = atomicMin(dist + 2 * h, nba);
-        const unsigned oldb = atomicMin(dist + 2 * h + 1, nbb);
-        const bool ia = nba < olda, ib = nbb < oldb;
-        if ((ia || ib) && !(h < F && h != src)) {
-          const unsigned bit = 1u << (h & 31);
-          if ((ia && nba < thr) || (ib && nbb < thr)) {
-            const unsigned prev = atomicOr(near + (h >> 5), bit);
-            if (!(prev & bit)) pm |= 1u << j;
-          }
-          if ((ia && nba >= thr) || (ib && nbb >= thr)) atomicOr(far + (h >> 5), bit);
-        }
-      }
-      while (pm) {
-        const int j = __ffs(pm) - 1;
-        pm &= pm - 1;
-        ++pushes;
-        ring_push<BLOCK>(ring, qhead, qtail, static_cast<int>(r4[j].x), a.err, ovf);
-      }
-      base += 4;
-      if (base >= deg) break;
-      const int c0 = __ldg(a.g.row_ptr + v) + base;
-#pragma unroll
-      for (int j = 0; j < 4; ++j)
-        if (base + j < deg) {
-          r4[j] = __ldg(csra + c0 + j);
-          wb[j] = __ldg(&csrb[c0 + j].y);
-        }
-    }
-  }
-  expanded += valid ? 1u : 0u;
-  const int used = warp_sum(pushes);
-  __syncwarp();
-  if (lane == 0) atomicAdd(pending, -(reserve - used + items));
-}
-
-// smallest of a far node's two labels that are at or above thr (kInf if none)
-__device__ __forceinline__ unsigned pair_far_label(const unsigned* dist, int v, unsigned thr) {
-  const unsigned la = dist[2 * v], lb = dist[2 * v + 1];
-  const unsigned ca = la >= thr ? la : DT<float>::kInf;
-  const unsigned cb = lb >= thr ? lb : DT<float>::kInf;
-  return ca < cb ? ca : cb;
-}
-
-template <int BLOCK, bool SMEM>
-__global__ void __launch_bounds__(BLOCK, (1024 / BLOCK > 0 ? 1024 / BLOCK : 1)) k_sssp_nfq2(PathArgs a) {
-  using U = unsigned;
-  using R = unsigned short;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ int sh_task;
-  __shared__ int pending;
-  __shared__ U sh_min;
-  __shared__ unsigned qhead, qtail;
-  __shared__ int ovf;
-  const int n1 = a.g.n1;
-  const int nwords = (n1 + 31) >> 5;
-  unsigned char* base =
-      SMEM ? smem_raw
-           : static_cast<unsigned char*>(a.scratch) + static_cast<size_t>(blockIdx.x) * a.scratch_stride;
-  U* dist = reinterpret_cast<U*>(base);  // [v][2]: both scenarios' labels of node v
-  unsigned* near = reinterpret_cast<unsigned*>(base + align16(8 * static_cast<size_t>(n1)));
-  unsigned* far = near + nwords;
-  R* ring = reinterpret_cast<R*>(far + nwords);
-  const int lane = threadIdx.x & 31;
-  const int warp = threadIdx.x >> 5;
-  constexpr int kWarps = BLOCK / 32;
-  const int F = a.g.first_thru;
-  const int my_words = warp < nwords ? (nwords - warp + kWarps - 1) / kWarps : 0;
-  const float delta = static_cast<float>(a.nf_delta);
-  const int Z = a.num_sources;
-  const int s0 = a.task_begin / Z;            // the launch's slots [s0, s1)
-  const int s1 = (a.task_end + Z - 1) / Z;
-  const int npair_tasks = ((s1 - s0 + 1) / 2) * Z;
-
-  for (;;) {
-    __syncthreads();
-    if (threadIdx.x == 0) sh_task = atomicAdd(a.counter, 1);
-    __syncthreads();
-    const int q = sh_task;
-    if (q >= npair_tasks) break;
-    const int pp = q / Z;
-    const int o = q - pp * Z;
-    const int slot_a = s0 + 2 * pp;
-    const bool has_b = slot_a + 1 < s1;
-    const int slot_b = has_b ? slot_a + 1 : slot_a;
-    const int scen_a = a.scen_list ? a.scen_list[slot_a] : 0;
-    const int scen_b = a.scen_list ? a.scen_list[slot_b] : 0;
-    if (a.state && a.state[scen_a].done && a.state[scen_b].done) continue;
-    const int src = a.sources[o];
-    const uint2* e4a = a.e4 + static_cast<size_t>(scen_a) * n1 * 4;
-    const uint2* e4b = a.e4 + static_cast<size_t>(scen_b) * n1 * 4;
-    const uint2* csra = a.e32 + static_cast<size_t>(scen_a) * a.g.m;
-    const uint2* csrb = a.e32 + static_cast<size_t>(scen_b) * a.g.m;
-    unsigned expanded = 0;
-    unsigned polls = 0, batches = 0, scanned = 0;
-    int phases = 0;
-
-    for (int v = threadIdx.x; v < 2 * n1; v += BLOCK) dist[v] = DT<float>::kInf;
-    for (int i = threadIdx.x; i < 2 * nwords; i += BLOCK) near[i] = 0u;
-    for (int i = threadIdx.x; i < kQCap; i += BLOCK) ring[i] = QEmpty<R>::value;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      dist[2 * src] = 0u;
-      dist[2 * src + 1] = 0u;
-      near[src >> 5] = 1u << (src & 31);
-      pending = 1;
-      ring[0] = static_cast<R>(src);
-      qhead = 0u;
-      qtail = 1u;
-      ovf = 0;
-    }
-    __syncthreads();
-    U thr = __float_as_uint(delta);
-
-    for (;;) {  // phases
-      int idle = 0;
-      for (;;) {
-        int claimed_any = 0;
-        for (;;) {  // batches of up to 32 nodes from the ring
-          unsigned h = 0u;
-          int n = 0;
-          if (lane == 0) {
-            for (int tries = 0; tries < 64; ++tries) {
-              h = vload(&qhead);
-              const int avail = static_cast<int>(vload(&qtail) - h);
-              if (avail <= 0) break;
-              const int take = avail < 32 ? avail : 32;
-              if (atomicCAS(&qhead, h, h + static_cast<unsigned>(take)) == h) {
-                n = take;
-                break;
-              }
-            }
-          }
-          n = __shfl_sync(kFull, n, 0);
-          if (n == 0) break;
-          h = __shfl_sync(kFull, h, 0);
-          claimed_any = 1;
-          int v = 0;
-          bool valid = false;
-          if (lane < n) {
-            volatile R* sl = ring + ((h + static_cast<unsigned>(lane)) & (kQCap - 1));
-            int e = -1;
-            for (int spins = 0; spins <= kMaxSlotSpins; ++spins) {
-              const R qv = *sl;
-              if (qv != QEmpty<R>::value) {
-                *sl = QEmpty<R>::value;
-                e = qv;
-                break;
-              }
-            }
-            if (e >= 0) {
-              v = e;
-              const unsigned bit = 1u << (v & 31);
-              valid = (atomicAnd(near + (v >> 5), ~bit) & bit) != 0u;
-            } else {  // the entry never arrived: its node is found by the scan
-              atomicOr(a.err, kErrRounds);
-              *reinterpret_cast<volatile int*>(&ovf) = 1;
-            }
-          }
-          ++batches;
-          nfq2_expand<BLOCK>(a, e4a, e4b, csra, csrb, src, F, dist, near, far, thr, ring, &qhead,
-                             &qtail, &pending, &ovf, v, valid, expanded);
-        }
-        // nodes that found the ring full: this warp's bitmap words
-        const int scan_words = __shfl_sync(kFull, vload(&ovf), 0) ? my_words : 0;
-        for (int j0 = 0; j0 < scan_words; j0 += 32) {
-          const int j = j0 + lane;
-          const int wi = warp + j * kWarps;
-          unsigned word = 0u;
-          if (j < my_words) {
-            word = vload(near + wi);
-            if (word) word = atomicExch(near + wi, 0u);
-          }
-          const int cnt = __popc(word);
-          int incl = cnt;
-#pragma unroll
-          for (int ofs = 1; ofs < 32; ofs <<= 1) {
-            const int y = __shfl_up_sync(kFull, incl, ofs);
-            if (lane >= ofs) incl += y;
-          }
-          const int total = __shfl_sync(kFull, incl, 31);
-          if (total == 0) continue;
-          claimed_any = 1;
-          for (int b = 0; b < total; b += 32) {
-            const int jj = b + lane;
-            int owner = 0;
-#pragma unroll
-            for (int step = 16; step >= 1; step >>= 1) {
-              const int probe = __shfl_sync(kFull, incl, owner + step - 1);
-              if (probe <= jj) owner += step;
-            }
-            owner &= 31;
-            const unsigned ow = __shfl_sync(kFull, word, owner);
-            const int oincl = __shfl_sync(kFull, incl, owner);
-            const bool valid = jj < total;
-            int v = 0;
-            if (valid)
-              v = ((warp + (j0 + owner) * kWarps) << 5) + nth_set_bit(ow, jj - (oincl - __popc(ow)));
-            ++batches;
-            scanned += valid ? 1u : 0u;
-            nfq2_expand<BLOCK>(a, e4a, e4b, csra, csrb, src, F, dist, near, far, thr, ring,
-                               &qhead, &qtail, &pending, &ovf, v, valid, expanded);
-          }
-        }
-        if (!claimed_any) {
-          if (__shfl_sync(kFull, vload(&pending), 0) <= 0) break;
-          ++polls;
-          if (++idle > kMaxIdlePolls) {
-            if (lane == 0) atomicOr(a.err, kErrRounds);
-            break;
-          }
-          __nanosleep(32);
-        }
-      }
-      __syncthreads();
-      int left = 0;
-      for (int i = threadIdx.x; i < nwords; i += BLOCK) left |= (near[i] != 0u);
-      if (__syncthreads_or(left)) {  // a warp left early: recount and resume
-        if (threadIdx.x == 0) {
-          pending = 0;
-          ovf = 1;
-        }
-        __syncthreads();
-        int c = 0;
-        for (int i = threadIdx.x; i < nwords; i += BLOCK) c += __popc(near[i]);
-        c = warp_sum(c);
-        if (lane == 0) atomicAdd(&pending, c);
-        __syncthreads();
-        if (++phases > a.max_rounds) {
-          if (threadIdx.x == 0) atomicOr(a.err, kErrRounds);
-          break;
-        }
-        continue;
-      }
-      if (threadIdx.x == 0) {
-        sh_min = DT<float>::kInf;
-        ovf = 0;
-      }
-      __syncthreads();
-      // phase step over the pair: a far node counts with its smallest label at
-      // or above the threshold (the other scenario may have settled it below)
-      U mn = DT<float>::kInf;
-      for (int i = threadIdx.x; i < nwords; i += BLOCK) {
-        const unsigned w = far[i];
-        if (!w) continue;
-        unsigned keep = 0u, ww = w;
-        while (ww) {
-          const int bpos = __ffs(ww) - 1;
-          ww &= ww - 1;
-          const U c = pair_far_label(dist, (i << 5) + bpos, thr);
-          if (c != DT<float>::kInf) {
-            keep |= 1u << bpos;
-            if (c < mn) mn = c;
-          }
-        }
-        if (keep != w) far[i] = keep;
-      }
-      if (mn != DT<float>::kInf) atomicMin(&sh_min, mn);
-      __syncthreads();
-      const U fmin = sh_min;
-      if (fmin == DT<float>::kInf) break;  // nothing left: labels are final
-      const U thr_old = thr;
-      thr = __float_as_uint(__fadd_rn(__uint_as_float(fmin), delta));
-      if (thr <= fmin) thr = fmin + 1;
-      int moved = 0;
-      for (int i = threadIdx.x; i < nwords; i += BLOCK) {
-        const unsigned w = far[i];
-        if (!w) continue;
-        unsigned take = 0u, ww = w;
-        while (ww) {
-          const int bpos = __ffs(ww) - 1;
-          ww &= ww - 1;
-          if (pair_far_label(dist, (i << 5) + bpos, thr_old) < thr) take |= 1u << bpos;
-        }
-        if (take) {
-          far[i] = w & ~take;
-          near[i] = take;
-          moved += __popc(take);
-          unsigned tt = take;
-          while (tt) {
-            const int bpos = __ffs(tt) - 1;
-            tt &= tt - 1;
-            ring_push<BLOCK>(ring, &qhead, &qtail, (i << 5) + bpos, a.err, &ovf);
-          }
-        }
-      }
-      if (threadIdx.x == 0) pending = 0;
-      __syncthreads();
-      moved = warp_sum(moved);
-      if (lane == 0 && moved) atomicAdd(&pending, moved);
-      __syncthreads();
-      if (++phases > a.max_rounds) {
-        if (threadIdx.x == 0) atomicOr(a.err, kErrRounds);
-        break;
-      }
-    }
-    float* outa = static_cast<float*>(a.dist) +
-                  (static_cast<size_t>(slot_a) * Z + o - a.task_begin) * n1;
-    float* outb = static_cast<float*>(a.dist) +
-                  (static_cast<size_t>(slot_b) * Z + o - a.task_begin) * n1;
-    for (int v = threadIdx.x; v < n1; v += BLOCK) {
-      outa[v] = __uint_as_float(dist[2 * v]);
-      if (has_b) outb[v] = __uint_as_float(dist[2 * v + 1]);
-    }
-    if (a.stats) {
-      for (int ofs = 16; ofs >= 1; ofs >>= 1) expanded += __shfl_down_sync(kFull, expanded, ofs);
-      if (lane == 0) {
-        atomicAdd(a.stats + 2, static_cast<unsigned long long>(expanded));
-        atomicAdd(a.stats + 3, static_cast<unsigned long long>(polls));
-        atomicAdd(a.stats + 4, static_cast<unsigned long long>(batches));
-        atomicAdd(a.stats + 5, static_cast<unsigned long long>(scanned));
-      }
-      if (threadIdx.x == 0) {
-        atomicAdd(a.stats + 0, static_cast<unsigned long long>(phases));
-        atomicAdd(a.stats + 1, 1ull);
-      }
-    }
-  }
-}
-
 constexpr unsigned short kNoParent16 = 0xffffu;  // node ids are below 65535 in the compact layout
 
 template <bool COMPACT>
@@ -2314,10 +1934,6 @@ using PathKernel = void (*)(PathArgs);
 
 template <typename T, int BLOCK, bool SMEM>
 PathKernel sssp_kernel(int variant) {
-  if (variant == kSsspNearFarQueuePair) {
-    if constexpr (std::is_same<T, float>::value) return k_sssp_nfq2<BLOCK, SMEM>;
-    return k_sssp_nfq<T, BLOCK, SMEM, unsigned short>;  // FP64 labels: one scenario per task
-  }
   if (variant == kSsspRounds) return k_sssp<T, BLOCK, SMEM>;
   if (variant == kSsspAsync) return k_sssp_async<T, BLOCK, SMEM>;
   if (variant == kSsspNearFarQueue) return k_sssp_nfq<T, BLOCK, SMEM, unsigned short>;
@@ -2353,11 +1969,8 @@ size_t sssp_smem_bytes(int n1, bool fp64, int variant) {
   const size_t words = (static_cast<size_t>(n1) + 31) / 32;
   const size_t ring = variant == kSsspNearFarQueue       ? sizeof(unsigned short) * kQCap
                       : variant == kSsspNearFarQueueWide ? sizeof(unsigned) * kQCap
-                      : variant == kSsspNearFarQueuePair ? sizeof(unsigned short) * kQCap
                                                          : 0;
-  // the pair kernel holds two FP32 labels per node (the FP64 queue layout)
-  const size_t label = fp64 || variant == kSsspNearFarQueuePair ? 8 : 4;
-  return align16(align16(label * static_cast<size_t>(n1)) + 2 * 4 * words + ring);
+  return align16(align16((fp64 ? 8 : 4) * static_cast<size_t>(n1)) + 2 * 4 * words + ring);
 }
 
 // Both sizes are also the stride between CTAs' slices of the global-memory
@@ -2379,9 +1992,7 @@ int max_smem_optin(int device) {
 cudaError_t launch_sssp(const PathArgs& a, bool fp64, int grid, int block, bool smem,
                         int variant, cudaStream_t s) {
   // FP32 paths of the queue variant read the padded records
-  if ((variant == kSsspNearFarQueue || variant == kSsspNearFarQueueWide ||
-       variant == kSsspNearFarQueuePair) &&
-      !fp64 && !a.e4)
+  if ((variant == kSsspNearFarQueue || variant == kSsspNearFarQueueWide) && !fp64 && !a.e4)
     return cudaErrorInvalidValue;
   const size_t bytes = sssp_smem_bytes(a.g.n1, fp64, variant);
 #define TAPGPU_SSSP_CASE(B)                                                              \

@@ -162,9 +162,6 @@ enum : int {
   kSsspNearFar = 3, // asynchronous near set below a rising threshold (k_sssp_nf)
   kSsspNearFarQueue = 4,  // near-far with a FIFO ring of near nodes (k_sssp_nfq)
   kSsspNearFarQueueWide = 5,  // the same with 32-bit ring entries (chosen above 65535 nodes)
-  kSsspNearFarQueuePair = 6,  // the queue kernel on two scenarios of one origin at once
-                              // (k_sssp_nfq2: FP32 paths, at most 65535 nodes; FP64 labels
-                              // run variant 4)
 };
 constexpr int kQueueSlots = 1024;  // ring slots of k_sssp_nfq
 cudaError_t launch_sssp(const PathArgs& a, bool fp64, int grid, int block, bool smem,

@@ -189,8 +189,7 @@ PathArgs Ctx::path_args(int nscen_slots) const {
   a.scratch_stride = 0;
   a.stats = timing ? path_stats : nullptr;
   a.nf_delta = nf_delta;
-  a.e4 = (!fp64 && (sssp_variant == kSsspNearFarQueue || sssp_variant == kSsspNearFarQueueWide ||
-                    sssp_variant == kSsspNearFarQueuePair))
+  a.e4 = (!fp64 && (sssp_variant == kSsspNearFarQueue || sssp_variant == kSsspNearFarQueueWide))
              ? e4
              : nullptr;
   return a;
@@ -324,24 +323,19 @@ int Ctx::plan_launches() {
   num_sms = prop.multiProcessorCount;
   const int optin = max_smem_optin(device);
   ls_mode = opt.line_search == kLsExact ? kLsExact : kLsReference;
-  sssp_variant = (opt.sssp_variant >= kSsspRounds && opt.sssp_variant <= kSsspNearFarQueue) ||
-                         opt.sssp_variant == kSsspNearFarQueuePair
+  sssp_variant = (opt.sssp_variant >= kSsspRounds && opt.sssp_variant <= kSsspNearFarQueue)
                      ? opt.sssp_variant
                      : kSsspNearFarQueue;
-  // the pair kernel runs FP32 labels of 16-bit nodes, and a label chunk must
-  // hold two scenarios' origins; otherwise the queue kernel runs
-  if (sssp_variant == kSsspNearFarQueuePair &&
-      (fp64 || !deg16 || dist_tasks < 2 * static_cast<int64_t>(std::max(Z, 1))))
-    sssp_variant = kSsspNearFarQueue;
   // the ring of the queue variant holds 16-bit node ids, and its padded
   // records 16-bit heads and degrees
   if (sssp_variant == kSsspNearFarQueue && !deg16) sssp_variant = kSsspNearFarQueueWide;
-  const bool queue = sssp_variant == kSsspNearFarQueue || sssp_variant == kSsspNearFarQueueWide ||
-                     sssp_variant == kSsspNearFarQueuePair;
-  const bool nf = sssp_variant == kSsspNearFar || queue;
+  const bool nf = sssp_variant == kSsspNearFar || sssp_variant == kSsspNearFarQueue ||
+                  sssp_variant == kSsspNearFarQueueWide;
   sssp_block = opt.sssp_block > 0 ? opt.sssp_block : (nf ? 256 : 512);
   // the ring keeps one free slot per thread
-  if (queue && sssp_block >= kQueueSlots) sssp_block = 256;
+  if ((sssp_variant == kSsspNearFarQueue || sssp_variant == kSsspNearFarQueueWide) &&
+      sssp_block >= kQueueSlots)
+    sssp_block = 256;
   aon_block = opt.aon_block > 0 ? opt.aon_block : 1024;
   // leave room for the kernels' static shared memory (a few words)
   const size_t room = optin > 1024 ? static_cast<size_t>(optin - 1024) : 0;
@@ -369,15 +363,8 @@ int Ctx::plan_launches() {
 int Ctx::enqueue_paths(int nscen, bool load, const uint2* e32p, const uint2* r32p, const double* w64p,
                        unsigned long long* ydst, bool use_state) {
   const int64_t tasks = static_cast<int64_t>(nscen) * Z;
-  // the pair kernel's chunks hold whole pairs of scenario slots
-  const bool pairs = sssp_variant == kSsspNearFarQueuePair && Z > 0;
-  const int64_t step = pairs ? (dist_tasks / (2 * Z)) * (2 * Z) : dist_tasks;
-  if (step < 1) {
-    set_message("the label buffer holds fewer tasks than two scenarios' origins");
-    return TAPGPU_ERR_UNSUPPORTED;
-  }
-  for (int64_t t0 = 0; t0 < tasks; t0 += step) {
-    const int64_t t1 = std::min(tasks, t0 + step);
+  for (int64_t t0 = 0; t0 < tasks; t0 += dist_tasks) {
+    const int64_t t1 = std::min(tasks, t0 + dist_tasks);
     PathArgs a = path_args(nscen);
     if (a.e4) a.e4 = e32p == e32 ? e4 : (e32p == api_e32 ? api_e4 : nullptr);
     a.e32 = e32p;
@@ -398,9 +385,7 @@ int Ctx::enqueue_paths(int nscen, bool load, const uint2* e32p, const uint2* r32
     TG_CUDA(cudaMemsetAsync(counters, 0, 2 * sizeof(int), stream));
     a.counter = counters;
     if (measuring) TG_TRY(mark(0, true));
-    // pair tasks: (pair of scenario slots, origin)
-    const int ptask = pairs ? static_cast<int>((((t1 - t0) / Z + 1) / 2) * Z) : ntask;
-    TG_CUDA(launch_sssp(a, fp64, std::min(sssp_grid, ptask), sssp_block, sssp_smem, sssp_variant,
+    TG_CUDA(launch_sssp(a, fp64, std::min(sssp_grid, ntask), sssp_block, sssp_smem, sssp_variant,
                         stream));
     if (measuring) TG_TRY(mark(0, false));
     a.counter = counters + 1;
@@ -777,12 +762,6 @@ static int create_impl(const tapgpu_network* net, const tapgpu_demand* dem,
   TG_CUDA(cudaMemcpy(c->sources, src.data(), sizeof(int) * src.size(), cudaMemcpyHostToDevice));
 
   TG_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-  // tasks of one label chunk (the buffer itself follows the launch plan)
-  const size_t tb = static_cast<size_t>(n1) * (c->fp64 ? 8 : 4);
-  int64_t chunk = opt.chunk_tasks > 0 ? opt.chunk_tasks
-                                      : std::max<int64_t>(1, (int64_t(2) << 30) / static_cast<int64_t>(tb));
-  chunk = std::max<int64_t>(1, std::min<int64_t>(chunk, 1 << 30));
-  c->dist_tasks = std::min<int64_t>(chunk, std::max<int64_t>(Z, 1) * 4096);
   TG_TRY(c->plan_launches());
   TG_TRY(c->alloc_n(&c->counters, 2));
   TG_TRY(c->alloc_n(&c->err, 1));
@@ -792,6 +771,11 @@ static int create_impl(const tapgpu_network* net, const tapgpu_demand* dem,
   TG_CUDA(cudaMemset(c->path_stats, 0, 8 * sizeof(unsigned long long)));
 
   // shortest-path label scratch between the two path kernels
+  const size_t tb = static_cast<size_t>(n1) * (c->fp64 ? 8 : 4);
+  int64_t chunk = opt.chunk_tasks > 0 ? opt.chunk_tasks
+                                      : std::max<int64_t>(1, (int64_t(2) << 30) / static_cast<int64_t>(tb));
+  chunk = std::max<int64_t>(1, std::min<int64_t>(chunk, 1 << 30));
+  c->dist_tasks = std::min<int64_t>(chunk, std::max<int64_t>(Z, 1) * 4096);
   TG_TRY(c->alloc(&c->dist, tb * c->dist_tasks));
   TG_TRY(c->alloc_n(&c->api_e32, M));
   TG_TRY(c->alloc_n(&c->api_e4, static_cast<size_t>(n1) * 4));
