@@ -213,3 +213,39 @@ def test_adjoint_grid10k_random_links(built_lib):
             assert abs(fd - g[a]) <= 1e-3 * abs(g[a]), (a, fd, g[a])
         else:
             assert abs(fd - g[a]) <= 1e-6 * gmax, (a, fd, g[a])
+
+
+def test_screening_ranks_c3_upgrades_like_full_resolves(built_lib):
+    """The use the gradient serves: screening candidate upgrades before any
+    full re-solve.  On the 10k-node network, 12 single-link upgrades (+25 %
+    capacity; the 6 links of most negative dVHT/dcapacity after 50
+    iterations and 6 random loaded links) are ranked by the first-order
+    estimate and by re-solving each to relative gap 2e-5 from the base
+    equilibrium (one batch).  The rank correlation is high and the estimate
+    picks the best upgrade; magnitudes are first-order (measured in FP64 on
+    16 candidates: Spearman 0.92, estimates 1.5-4x the re-solved change)."""
+    from scipy.stats import spearmanr
+
+    from traffic_assignment_gb300 import adjoint
+
+    net, dem = synth.make_grid10k()
+    _, _, g = adjoint.screen_upgrades(net, dem, [[0]], [[0.0]], iters=50)
+    with Solver(net, dem, precision="fp32") as s:
+        base = s.solve(target_relgap=2e-5, max_iters=20000)
+        xb, _ = s.flows()
+    rng = np.random.default_rng(11)
+    top = np.argsort(g)[:6]
+    loaded = np.setdiff1d(np.nonzero(xb > 100)[0], top)
+    cands = [[int(k)] for k in np.concatenate([top, rng.choice(loaded, 6, replace=False)])]
+    est, _, _ = adjoint.screen_upgrades(net, dem, cands, [[0.25]] * len(cands), iters=50)
+    scen = [synth.Scenario(f"c{i}", np.array(c), net.capacity[c] * 1.25)
+            for i, c in enumerate(cands)]
+    with Solver(net, dem, precision="fp32") as s:
+        res = s.solve_scenarios(scen, target_relgap=2e-5, max_iters=20000, x0=xb)
+    dv = np.array([r["total_cost"] for r in res]) - base["total_cost"]
+    assert all(r["error_bits"] == 0 and r["relgap"] <= 2e-5 for r in res)
+    rho = spearmanr(est, dv).correlation
+    assert rho >= 0.75, (rho, est, dv)
+    assert int(np.argmin(dv)) in np.argsort(est)[:3]
+    big = np.abs(est) >= 1000
+    assert np.all(dv[big] < 0)
