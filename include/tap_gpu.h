@@ -236,10 +236,13 @@ typedef struct tapgpu_options_s {
   int record_tape;       /* keep per-iteration flows and directions for the adjoint */
   int tape_capacity;     /* iterations kept on the tape */
   int global_scratch;    /* 1: per-CTA labels in global memory even when shared memory fits */
-  int sssp_variant;      /* 0 default (4, or 3 above 65535 nodes); 1 bulk-synchronous
+  int sssp_variant;      /* 0 default (6 up to 4096 nodes and links, else 4, or its 32-bit
+                            ring form above 65535 nodes); 1 bulk-synchronous
                             rounds; 2 asynchronous warp-owned frontier; 3 asynchronous near
                             set below a rising threshold; 4 as 3 with a FIFO ring of near
-                            nodes (networks of at most 65535 nodes) */
+                            nodes (networks of at most 65535 nodes); 6 Bellman-Ford
+                            sweeps over the edge list held in shared memory (the default
+                            for networks of at most 4096 nodes and 4096 links) */
   double nf_delta;       /* threshold step of variants 3 and 4 in cost units; 0 = 16 x mean
                             link cost */
   int line_search;       /* 0: the reference's 2^-k rule; 1: exact root of the directional

@@ -46,7 +46,7 @@ def test_aon_matches_oracle(built_lib, grid416):
             assert _rel(y, ref) < 1e-12
 
 
-VARIANTS = ["rounds", "async", "nearfar", "nearfar_queue"]
+VARIANTS = ["rounds", "async", "nearfar", "nearfar_queue", "small"]
 
 
 @pytest.mark.parametrize("variant", VARIANTS)

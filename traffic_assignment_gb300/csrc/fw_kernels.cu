@@ -1220,6 +1220,87 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
   }
 }
 
+// ---------------------------------------------------------------------------
+// k_sssp_small: Bellman-Ford sweeps over an edge list held in shared memory
+// ---------------------------------------------------------------------------
+// For small networks, whose tasks are too small to keep a queue busy (a
+// 416-node network has a few dozen origins: one task per SM and nothing to
+// hide a queue's latency), the CTA copies the edge list {tail, head,
+// weight} of its task's scenario into shared memory and relaxes every edge
+// in sweeps until one changes no label.  Labels improve in place during a
+// sweep (atomicMin), so an improvement travels along later edges of the same
+// sweep; a sweep that changes nothing ends the task.  The labels are the
+// same least fixed point of the relaxations as every other schedule's.
+template <typename T, int BLOCK, bool SMEM>
+__global__ void __launch_bounds__(BLOCK) k_sssp_small(PathArgs a) {
+  using U = typename DT<T>::U;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int sh_task;
+  const int n1 = a.g.n1, m = a.g.m;
+  unsigned char* base =
+      SMEM ? smem_raw
+           : static_cast<unsigned char*>(a.scratch) + static_cast<size_t>(blockIdx.x) * a.scratch_stride;
+  U* dist = reinterpret_cast<U*>(base);
+  int* et = reinterpret_cast<int*>(base + align16(sizeof(U) * n1));
+  int* eh = et + m;
+  T* ew = reinterpret_cast<T*>(base + align16(sizeof(U) * n1) + align16(8 * static_cast<size_t>(m)));
+  const int F = a.g.first_thru;
+  for (int k = threadIdx.x; k < m; k += BLOCK) et[k] = __ldg(a.g.tail + k);
+  int staged = -1;  // scenario whose weights are in shared memory
+
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) sh_task = atomicAdd(a.counter, 1) + a.task_begin;
+    __syncthreads();
+    const int task = sh_task;
+    if (task >= a.task_end) break;
+    const int slot = task / a.num_sources;
+    const int scen = a.scen_list ? a.scen_list[slot] : 0;
+    if (a.state && a.state[scen].done) continue;
+    const int src = a.sources[task - slot * a.num_sources];
+    if (scen != staged) {  // (uniform)
+      const Edges<T> ed = edges_of<T>(a, scen);
+      for (int k = threadIdx.x; k < m; k += BLOCK) {
+        int h;
+        T w;
+        ed.load(k, h, w);
+        eh[k] = h;
+        ew[k] = w;
+      }
+      staged = scen;
+    }
+    for (int v = threadIdx.x; v < n1; v += BLOCK) dist[v] = DT<T>::kInf;
+    __syncthreads();
+    if (threadIdx.x == 0) dist[src] = DT<T>::bits(T(0));
+    __syncthreads();
+    int sweeps = 0;
+    for (;;) {
+      int changed = 0;
+      for (int k = threadIdx.x; k < m; k += BLOCK) {
+        const int u = et[k];
+        if (u < F && u != src) continue;  // zones are never passed through
+        const U du = vload(dist + u);
+        if (du == DT<T>::kInf) continue;
+        const U nb = DT<T>::bits(DT<T>::add(DT<T>::val(du), ew[k]));
+        const int h = eh[k];
+        if (nb < vload(dist + h) && nb < atomicMin(dist + h, nb)) changed = 1;
+      }
+      ++sweeps;
+      if (!__syncthreads_or(changed)) break;
+      if (sweeps > n1 + 1) {  // (cannot happen with non-negative weights)
+        if (threadIdx.x == 0) atomicOr(a.err, kErrRounds);
+        break;
+      }
+    }
+    T* out = static_cast<T*>(a.dist) + static_cast<size_t>(task - a.task_begin) * n1;
+    for (int v = threadIdx.x; v < n1; v += BLOCK) out[v] = DT<T>::val(dist[v]);
+    if (a.stats && threadIdx.x == 0) {
+      atomicAdd(a.stats + 0, static_cast<unsigned long long>(sweeps));
+      atomicAdd(a.stats + 1, 1ull);
+    }
+  }
+}
+
 constexpr unsigned short kNoParent16 = 0xffffu;  // node ids are below 65535 in the compact layout
 
 template <bool COMPACT>
@@ -1934,6 +2015,7 @@ using PathKernel = void (*)(PathArgs);
 
 template <typename T, int BLOCK, bool SMEM>
 PathKernel sssp_kernel(int variant) {
+  if (variant == kSsspSmall) return k_sssp_small<T, BLOCK, SMEM>;
   if (variant == kSsspRounds) return k_sssp<T, BLOCK, SMEM>;
   if (variant == kSsspAsync) return k_sssp_async<T, BLOCK, SMEM>;
   if (variant == kSsspNearFarQueue) return k_sssp_nfq<T, BLOCK, SMEM, unsigned short>;
@@ -1965,7 +2047,10 @@ cudaError_t launch_aon_t(const PathArgs& a, int grid, size_t smem, cudaStream_t 
 
 }  // namespace
 
-size_t sssp_smem_bytes(int n1, bool fp64, int variant) {
+size_t sssp_smem_bytes(int n1, bool fp64, int variant, int m) {
+  if (variant == kSsspSmall)  // labels, then tails and heads, then weights
+    return align16(align16((fp64 ? 8 : 4) * static_cast<size_t>(n1)) +
+                   align16(8 * static_cast<size_t>(m)) + (fp64 ? 8 : 4) * static_cast<size_t>(m));
   const size_t words = (static_cast<size_t>(n1) + 31) / 32;
   const size_t ring = variant == kSsspNearFarQueue       ? sizeof(unsigned short) * kQCap
                       : variant == kSsspNearFarQueueWide ? sizeof(unsigned) * kQCap
@@ -1994,7 +2079,7 @@ cudaError_t launch_sssp(const PathArgs& a, bool fp64, int grid, int block, bool 
   // FP32 paths of the queue variant read the padded records
   if ((variant == kSsspNearFarQueue || variant == kSsspNearFarQueueWide) && !fp64 && !a.e4)
     return cudaErrorInvalidValue;
-  const size_t bytes = sssp_smem_bytes(a.g.n1, fp64, variant);
+  const size_t bytes = sssp_smem_bytes(a.g.n1, fp64, variant, a.g.m);
 #define TAPGPU_SSSP_CASE(B)                                                              \
   if (block == B) {                                                                      \
     if (fp64) return smem ? launch_sssp_t<double, B, true>(a, grid, bytes, variant, s)   \
@@ -2050,8 +2135,8 @@ int occ_aon_t(size_t smem) {
   return n;
 }
 
-int sssp_occupancy(bool fp64, int block, bool smem, int n1, int variant) {
-  const size_t bytes = sssp_smem_bytes(n1, fp64, variant);
+int sssp_occupancy(bool fp64, int block, bool smem, int n1, int variant, int m) {
+  const size_t bytes = sssp_smem_bytes(n1, fp64, variant, m);
 #define TAPGPU_OCC(B)                                                                     \
   if (block == B) {                                                                       \
     if (fp64) return smem ? occ_sssp_t<double, B, true>(bytes, variant)                   \

@@ -151,7 +151,8 @@ struct LinkArgs {
 };
 
 // launch helpers (implemented in fw_kernels.cu)
-size_t sssp_smem_bytes(int n1, bool fp64, int variant = 0);
+// (m: links, used by the small-network variant, whose edge list is held too)
+size_t sssp_smem_bytes(int n1, bool fp64, int variant = 0, int m = 0);
 size_t aon_smem_bytes(int n1, bool fp64);
 bool aon_compact(int n1, bool fp64);  // 10-byte-per-node loading layout
 int max_smem_optin(int device);
@@ -162,7 +163,10 @@ enum : int {
   kSsspNearFar = 3, // asynchronous near set below a rising threshold (k_sssp_nf)
   kSsspNearFarQueue = 4,  // near-far with a FIFO ring of near nodes (k_sssp_nfq)
   kSsspNearFarQueueWide = 5,  // the same with 32-bit ring entries (chosen above 65535 nodes)
+  kSsspSmall = 6,   // Bellman-Ford sweeps over the edge list in shared memory (k_sssp_small;
+                    // chosen for networks of at most kSmallNet nodes and links)
 };
+constexpr int kSmallNet = 4096;
 constexpr int kQueueSlots = 1024;  // ring slots of k_sssp_nfq
 cudaError_t launch_sssp(const PathArgs& a, bool fp64, int grid, int block, bool smem,
                         int variant, cudaStream_t s);
@@ -187,7 +191,8 @@ cudaError_t launch_param_rows(unsigned char* rows, const unsigned char* base, in
                               cudaStream_t s);
 // rows 1 .. nscen-1 of x [nscen][m] become copies of row 0
 cudaError_t launch_replicate_rows(double* x, int m, int nscen, int grid, cudaStream_t s);
-int sssp_occupancy(bool fp64, int block, bool smem, int n1, int variant);  // CTAs per SM
+int sssp_occupancy(bool fp64, int block, bool smem, int n1, int variant,
+                   int m = 0);  // CTAs per SM
 int aon_occupancy(bool fp64, int block, bool smem, int n1);
 
 }  // namespace tapgpu

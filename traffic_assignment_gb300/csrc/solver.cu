@@ -323,9 +323,13 @@ int Ctx::plan_launches() {
   num_sms = prop.multiProcessorCount;
   const int optin = max_smem_optin(device);
   ls_mode = opt.line_search == kLsExact ? kLsExact : kLsReference;
-  sssp_variant = (opt.sssp_variant >= kSsspRounds && opt.sssp_variant <= kSsspNearFarQueue)
+  // default: the edge-list sweeps for small networks (tasks too small to
+  // keep a queue busy), else the queue kernel
+  const bool small = n1 <= kSmallNet && M <= kSmallNet;
+  sssp_variant = (opt.sssp_variant >= kSsspRounds && opt.sssp_variant <= kSsspNearFarQueue) ||
+                         opt.sssp_variant == kSsspSmall
                      ? opt.sssp_variant
-                     : kSsspNearFarQueue;
+                     : (small ? kSsspSmall : kSsspNearFarQueue);
   // the ring of the queue variant holds 16-bit node ids, and its padded
   // records 16-bit heads and degrees
   if (sssp_variant == kSsspNearFarQueue && !deg16) sssp_variant = kSsspNearFarQueueWide;
@@ -339,9 +343,9 @@ int Ctx::plan_launches() {
   aon_block = opt.aon_block > 0 ? opt.aon_block : 1024;
   // leave room for the kernels' static shared memory (a few words)
   const size_t room = optin > 1024 ? static_cast<size_t>(optin - 1024) : 0;
-  sssp_smem = sssp_smem_bytes(n1, fp64, sssp_variant) <= room && !opt.global_scratch;
+  sssp_smem = sssp_smem_bytes(n1, fp64, sssp_variant, M) <= room && !opt.global_scratch;
   aon_smem = aon_smem_bytes(n1, fp64) <= room && !opt.global_scratch;
-  int so = sssp_occupancy(fp64, sssp_block, sssp_smem, n1, sssp_variant);
+  int so = sssp_occupancy(fp64, sssp_block, sssp_smem, n1, sssp_variant, M);
   int ao = aon_occupancy(fp64, aon_block, aon_smem, n1);
   if (so <= 0 || ao <= 0) {
     set_message("no resident CTA fits for the shortest-path kernels");
@@ -350,7 +354,7 @@ int Ctx::plan_launches() {
   sssp_grid = so * num_sms;
   aon_grid = ao * num_sms;
   size_t scratch = 0;
-  if (!sssp_smem) scratch = std::max(scratch, sssp_smem_bytes(n1, fp64, sssp_variant) * sssp_grid);
+  if (!sssp_smem) scratch = std::max(scratch, sssp_smem_bytes(n1, fp64, sssp_variant, M) * sssp_grid);
   if (!aon_smem) scratch = std::max(scratch, aon_smem_bytes(n1, fp64) * aon_grid);
   if (scratch) {
     TG_TRY(alloc(&path_scratch, scratch));
@@ -381,7 +385,7 @@ int Ctx::enqueue_paths(int nscen, bool load, const uint2* e32p, const uint2* r32
       a.dem.q_stride = 0;
     }
     const int ntask = static_cast<int>(t1 - t0);
-    a.scratch_stride = static_cast<long long>(sssp_smem_bytes(n1, fp64, sssp_variant));
+    a.scratch_stride = static_cast<long long>(sssp_smem_bytes(n1, fp64, sssp_variant, M));
     TG_CUDA(cudaMemsetAsync(counters, 0, 2 * sizeof(int), stream));
     a.counter = counters;
     if (measuring) TG_TRY(mark(0, true));
@@ -1474,13 +1478,13 @@ int tapgpu_sssp(tapgpu_ctx* ctx, const double* weights, const int64_t* srcs, int
     a.y_fx = c->api_yfx;
     a.nf_delta = c->api_nf_delta;
     const int optin = tapgpu::max_smem_optin(c->device);
-    const bool s_smem = tapgpu::sssp_smem_bytes(n1, true, c->sssp_variant) + 1024 <= static_cast<size_t>(optin);
-    const int occ = tapgpu::sssp_occupancy(true, c->sssp_block, s_smem, n1, c->sssp_variant);
+    const bool s_smem = tapgpu::sssp_smem_bytes(n1, true, c->sssp_variant, c->M) + 1024 <= static_cast<size_t>(optin);
+    const int occ = tapgpu::sssp_occupancy(true, c->sssp_block, s_smem, n1, c->sssp_variant, c->M);
     int grid = std::max(1, std::min(occ * c->num_sms, ns));
     if (!s_smem) {
-      const size_t need = tapgpu::sssp_smem_bytes(n1, true, c->sssp_variant) * static_cast<size_t>(grid);
+      const size_t need = tapgpu::sssp_smem_bytes(n1, true, c->sssp_variant, c->M) * static_cast<size_t>(grid);
       if (need > c->path_scratch_bytes) {
-        grid = std::max<int>(1, static_cast<int>(c->path_scratch_bytes / tapgpu::sssp_smem_bytes(n1, true, c->sssp_variant)));
+        grid = std::max<int>(1, static_cast<int>(c->path_scratch_bytes / tapgpu::sssp_smem_bytes(n1, true, c->sssp_variant, c->M)));
         if (c->path_scratch_bytes == 0) {
           rc = TAPGPU_ERR_UNSUPPORTED;
           break;
@@ -1489,7 +1493,7 @@ int tapgpu_sssp(tapgpu_ctx* ctx, const double* weights, const int64_t* srcs, int
     }
     cudaMemsetAsync(c->counters, 0, 2 * sizeof(int), c->stream);
     a.counter = c->counters;
-    a.scratch_stride = static_cast<long long>(tapgpu::sssp_smem_bytes(n1, true, c->sssp_variant));
+    a.scratch_stride = static_cast<long long>(tapgpu::sssp_smem_bytes(n1, true, c->sssp_variant, c->M));
     if (tapgpu::launch_sssp(a, true, grid, c->sssp_block, s_smem, c->sssp_variant, c->stream) !=
         cudaSuccess) {
       rc = TAPGPU_ERR_CUDA;
@@ -1667,7 +1671,7 @@ int tapgpu_profile_iteration(tapgpu_ctx* ctx, int reps, float* ms) {
     a.task_end = static_cast<int>(tasks);
     cudaMemsetAsync(c->counters, 0, 2 * sizeof(int), c->stream);
     a.counter = c->counters;
-    a.scratch_stride = static_cast<long long>(tapgpu::sssp_smem_bytes(c->n1, c->fp64, c->sssp_variant));
+    a.scratch_stride = static_cast<long long>(tapgpu::sssp_smem_bytes(c->n1, c->fp64, c->sssp_variant, c->M));
     a.e32 = c->fp64 ? nullptr : c->e32;
     a.r32 = c->fp64 ? nullptr : c->r32;
     a.w64 = c->fp64 ? c->w64 : nullptr;

@@ -76,7 +76,7 @@ class Solver:
         opt.tape_capacity = tape_capacity
         opt.global_scratch = 1 if global_scratch else 0
         opt.sssp_variant = {"default": 0, "rounds": 1, "async": 2, "nearfar": 3,
-                            "nearfar_queue": 4}[sssp_variant]
+                            "nearfar_queue": 4, "small": 6}[sssp_variant]
         opt.nf_delta = float(nf_delta)
         opt.line_search = {"reference": 0, "exact": 1}[line_search]
         opt.tape_checkpoint = int(tape_checkpoint)
