@@ -1790,6 +1790,60 @@ __device__ void ls_decide(ScenState& st, const double* tot, int first_e, int pas
   st.ls_next = first_e + kLsPerPass;
 }
 
+// One link's part of a line-search pass: pass 0 forms d = y - x (stored) and
+// adds the link's gap, VHT, objective and g(1) terms; every pass adds its
+// candidate steps' terms.
+__device__ __forceinline__ void ls_link(const LinkArgs& a, int scen, size_t off, const double* cap,
+                                        int k, int pass, int e0, double blo, double bhi,
+                                        double (&acc)[kNumSums]) {
+  const double x = a.x[off + k];
+  const size_t pk = lpi(a.lp, scen, k);
+  const double fft = a.lp.fft[pk], al = a.lp.alpha[pk], be = a.lp.beta[pk], c = cap[k];
+  const unsigned char ip = a.lp.ipow[pk];
+  // FP32-path mode, integer power: t(x + lam d) = fft + (fft alpha) (x/c + lam d/c)^beta
+  // with one division per link (FP64 mode keeps the reference's forms,
+  // tap/tap_functions.c:55-65, 112-126)
+  const bool ratio = a.ls_ratio && ip != 255;
+  const double ic = ratio ? 1.0 / c : 0.0;
+  const double A = fft * al;
+  double d;
+  if (pass == 0) {
+    const double y = static_cast<double>(static_cast<long long>(a.y_fx[off + k])) * a.inv_scale;
+    a.y_fx[off + k] = 0ull;
+    d = __dsub_rn(y, x);
+    a.d[off + k] = d;
+    const double t = a.t[off + k];
+    acc[0] = __dadd_rn(acc[0], __dmul_rn(t, d));
+    acc[1] = __dadd_rn(acc[1], __dmul_rn(x, t));
+    if (ratio) {
+      // x fft (1 + alpha / (beta + 1) (x/c)^beta) and t(x + d) d
+      const double r0 = x * ic;
+      acc[2] += x * (fft + A * bprf::int_pow_fast(r0, ip) * bprf::inv_int(ip + 1));
+      acc[3] += (fft + A * bprf::int_pow_fast(r0 + d * ic, ip)) * d;
+    } else {
+      acc[2] = __dadd_rn(acc[2], integral(fft, al, be, ip, c, x));
+      acc[3] = __dadd_rn(acc[3], __dmul_rn(bpr(fft, al, be, ip, c, __dadd_rn(x, d)), d));
+    }
+  } else {
+    d = a.d[off + k];
+  }
+  if (ratio) {
+    const double r0 = x * ic, rd = d * ic;
+#pragma unroll
+    for (int j = 0; j < kLsPerPass; ++j) {
+      const double lam = ls_candidate(a.ls_mode, e0, blo, bhi, j);
+      acc[4 + j] += (fft + A * bprf::int_pow_fast(r0 + lam * rd, ip)) * d;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < kLsPerPass; ++j) {
+      const double lam = ls_candidate(a.ls_mode, e0, blo, bhi, j);
+      const double q = __dadd_rn(x, __dmul_rn(lam, d));
+      acc[4 + j] = __dadd_rn(acc[4 + j], __dmul_rn(bpr(fft, al, be, ip, c, q), d));
+    }
+  }
+}
+
 // One line-search pass; pass 0 also forms d = y - x and the gap / objective /
 // VHT sums.  Candidates of this pass: 2^-(e0 .. e0+kLsPerPass-1).
 __global__ void __launch_bounds__(kLinkBlock) k_ls_pass(LinkArgs a) {
@@ -1806,54 +1860,8 @@ __global__ void __launch_bounds__(kLinkBlock) k_ls_pass(LinkArgs a) {
 #pragma unroll
   for (int i = 0; i < kNumSums; ++i) acc[i] = 0.0;
   const double* cap = a.cap + off;
-  for (int k = blockIdx.x * kLinkBlock + threadIdx.x; k < a.m; k += gridDim.x * kLinkBlock) {
-    const double x = a.x[off + k];
-    const size_t pk = lpi(a.lp, scen, k);
-    const double fft = a.lp.fft[pk], al = a.lp.alpha[pk], be = a.lp.beta[pk], c = cap[k];
-    const unsigned char ip = a.lp.ipow[pk];
-    // FP32-path mode, integer power: t(x + lam d) = fft + (fft alpha) (x/c + lam d/c)^beta
-    // with one division per link (FP64 mode keeps the reference's forms,
-    // tap/tap_functions.c:55-65, 112-126)
-    const bool ratio = a.ls_ratio && ip != 255;
-    const double ic = ratio ? 1.0 / c : 0.0;
-    const double A = fft * al;
-    double d;
-    if (a.pass == 0) {
-      const double y = static_cast<double>(static_cast<long long>(a.y_fx[off + k])) * a.inv_scale;
-      a.y_fx[off + k] = 0ull;
-      d = __dsub_rn(y, x);
-      a.d[off + k] = d;
-      const double t = a.t[off + k];
-      acc[0] = __dadd_rn(acc[0], __dmul_rn(t, d));
-      acc[1] = __dadd_rn(acc[1], __dmul_rn(x, t));
-      if (ratio) {
-        // x fft (1 + alpha / (beta + 1) (x/c)^beta) and t(x + d) d
-        const double r0 = x * ic;
-        acc[2] += x * (fft + A * bprf::int_pow_fast(r0, ip) * bprf::inv_int(ip + 1));
-        acc[3] += (fft + A * bprf::int_pow_fast(r0 + d * ic, ip)) * d;
-      } else {
-        acc[2] = __dadd_rn(acc[2], integral(fft, al, be, ip, c, x));
-        acc[3] = __dadd_rn(acc[3], __dmul_rn(bpr(fft, al, be, ip, c, __dadd_rn(x, d)), d));
-      }
-    } else {
-      d = a.d[off + k];
-    }
-    if (ratio) {
-      const double r0 = x * ic, rd = d * ic;
-#pragma unroll
-      for (int j = 0; j < kLsPerPass; ++j) {
-        const double lam = ls_candidate(a.ls_mode, e0, blo, bhi, j);
-        acc[4 + j] += (fft + A * bprf::int_pow_fast(r0 + lam * rd, ip)) * d;
-      }
-    } else {
-#pragma unroll
-      for (int j = 0; j < kLsPerPass; ++j) {
-        const double lam = ls_candidate(a.ls_mode, e0, blo, bhi, j);
-        const double q = __dadd_rn(x, __dmul_rn(lam, d));
-        acc[4 + j] = __dadd_rn(acc[4 + j], __dmul_rn(bpr(fft, al, be, ip, c, q), d));
-      }
-    }
-  }
+  for (int k = blockIdx.x * kLinkBlock + threadIdx.x; k < a.m; k += gridDim.x * kLinkBlock)
+    ls_link(a, scen, off, cap, k, a.pass, e0, blo, bhi, acc);
   block_sum<kNumSums, kLinkBlock>(acc, sh);
   double* part = a.partials + (static_cast<size_t>(scen) * gridDim.x + blockIdx.x) * kNumSums;
   if (threadIdx.x == 0) {
@@ -1875,14 +1883,13 @@ __global__ void __launch_bounds__(kLinkBlock) k_ls_pass(LinkArgs a) {
 }
 
 // Continue the halving sequence one candidate at a time up to the reference's
-// cap of 1000 halvings (never reached on valid inputs).  Single block.
-__global__ void __launch_bounds__(1024) k_ls_fallback(LinkArgs a) {
-  __shared__ double sh[32];
-  __shared__ int sh_found;
-  const int scen = scen_of(a);
-  ScenState& st = a.state[scen];
+// cap of 1000 halvings (never reached on valid inputs), by one block (any
+// size up to 1024 threads); every thread of the block calls it.
+__device__ void ls_fallback_block(const LinkArgs& a, int scen, ScenState& st, double* sh,
+                                  int* sh_found) {
   if (st.done || !st.ls_pending) return;
   if (a.ls_mode == kLsExact) {  // bracket already tight: interpolate
+    __syncthreads();            // every thread has read the state before it changes
     if (threadIdx.x == 0) {
       const double den = st.ls_glo - st.ls_ghi;
       st.lambda = den < 0 ? st.ls_lo + (st.ls_hi - st.ls_lo) * (st.ls_glo / den) : st.ls_lo;
@@ -1908,20 +1915,85 @@ __global__ void __launch_bounds__(1024) k_ls_fallback(LinkArgs a) {
     if (threadIdx.x == 0) {
       double t = 0.0;
       for (unsigned w = 0; w < blockDim.x / 32; ++w) t += sh[w];
-      sh_found = t <= 0 ? 1 : 0;
-      if (sh_found) {
+      *sh_found = t <= 0 ? 1 : 0;
+      if (*sh_found) {
         st.lambda = lam;
         st.ls_pending = 0;
       }
     }
     __syncthreads();
-    if (sh_found) return;
+    if (*sh_found) return;
   }
   if (threadIdx.x == 0) {
     st.lambda = 0.0;  // tap/tap_functions.c:506 returns lambda_left == 0
     st.ls_pending = 0;
     atomicOr(a.err, kErrLineSearch);
   }
+}
+
+__global__ void __launch_bounds__(1024) k_ls_fallback(LinkArgs a) {
+  __shared__ double sh[32];
+  __shared__ int sh_found;
+  const int scen = scen_of(a);
+  ls_fallback_block(a, scen, a.state[scen], sh, &sh_found);
+}
+
+// Where iteration `it` of a scenario writes its adjoint tape: every
+// direction, the flows only every ckpt_every iterations.
+struct TapeAt {
+  bool tape, ckpt;
+  size_t hoff, xoff;
+};
+__device__ __forceinline__ TapeAt tape_at(const LinkArgs& a, int scen, int it) {
+  TapeAt r;
+  r.tape = a.d_hist && it < a.hist_cap;
+  r.ckpt = r.tape && (it % a.ckpt_every == 0);
+  r.hoff = r.tape ? (static_cast<size_t>(scen) * a.hist_cap + it) * a.m : 0;
+  const size_t nck = static_cast<size_t>(a.hist_cap / a.ckpt_every + 1);
+  r.xoff = r.ckpt ? (static_cast<size_t>(scen) * nck + it / a.ckpt_every) * a.m : 0;
+  return r;
+}
+
+// x += lambda d on link k, its BPR cost and derivative, the next weights;
+// returns the link's x t (VHT term)
+__device__ __forceinline__ double step_link(const LinkArgs& a, int scen, size_t off, const double* cap,
+                                            int k, double lam, const TapeAt& tp) {
+  const double x0 = a.x[off + k];
+  const double d = a.d[off + k];
+  if (tp.tape) a.d_hist[tp.hoff + k] = d;
+  if (tp.ckpt) a.x_hist[tp.xoff + k] = x0;
+  const double x = __dadd_rn(x0, __dmul_rn(lam, d));
+  a.x[off + k] = x;
+  const size_t pk = lpi(a.lp, scen, k);
+  const double fft = a.lp.fft[pk], al = a.lp.alpha[pk], be = a.lp.beta[pk], c = cap[k];
+  const unsigned char ip = a.lp.ipow[pk];
+  const double t = bpr(fft, al, be, ip, c, x);
+  a.t[off + k] = t;
+  if (a.dtdx) a.dtdx[off + k] = bpr_dq(fft, al, be, ip, c, x);
+  write_weights(a, scen, k, t);
+  return __dmul_rn(x, t);
+}
+
+// the iteration's bookkeeping once the step's VHT is summed (one thread)
+__device__ __forceinline__ void step_finish(const LinkArgs& a, int scen, ScenState& st, int it,
+                                            double lam, const TapeAt& tp, double vht) {
+  st.vht_end = vht;
+  if (tp.tape) a.lam_hist[static_cast<size_t>(scen) * a.hist_cap + it] = lam;
+  if (a.trace && it < a.trace_cap) {
+    double* r = a.trace + (static_cast<size_t>(scen) * a.trace_cap + it) * kTraceCols;
+    r[0] = st.obj;
+    r[1] = st.relgap;
+    r[2] = st.avg_excess;
+    r[3] = st.vht;
+    r[4] = lam;
+    r[5] = st.gap;
+    r[6] = it + 1;
+    r[7] = st.g0;
+  }
+  st.iter = it + 1;
+  if ((st.max_iters > 0 && st.iter >= st.max_iters) ||
+      (st.target_relgap > 0 && !(st.relgap > st.target_relgap)))
+    st.done = 1;
 }
 
 // x += lambda d; t = BPR(x); next weights; iteration bookkeeping.
@@ -1933,30 +2005,11 @@ __global__ void __launch_bounds__(kLinkBlock) k_step(LinkArgs a) {
   const size_t off = static_cast<size_t>(scen) * a.m;
   const double lam = st.lambda;
   const int it = st.iter;
-  // adjoint tape: every direction, the flows only every ckpt_every iterations
-  const bool tape = a.d_hist && it < a.hist_cap;
-  const bool ckpt = tape && (it % a.ckpt_every == 0);
-  const size_t hoff = tape ? (static_cast<size_t>(scen) * a.hist_cap + it) * a.m : 0;
-  const size_t nck = static_cast<size_t>(a.hist_cap / a.ckpt_every + 1);
-  const size_t xoff = ckpt ? (static_cast<size_t>(scen) * nck + it / a.ckpt_every) * a.m : 0;
+  const TapeAt tp = tape_at(a, scen, it);
   const double* cap = a.cap + off;
   double acc[1] = {0.0};
-  for (int k = blockIdx.x * kLinkBlock + threadIdx.x; k < a.m; k += gridDim.x * kLinkBlock) {
-    const double x0 = a.x[off + k];
-    const double d = a.d[off + k];
-    if (tape) a.d_hist[hoff + k] = d;
-    if (ckpt) a.x_hist[xoff + k] = x0;
-    const double x = __dadd_rn(x0, __dmul_rn(lam, d));
-    a.x[off + k] = x;
-    const size_t pk = lpi(a.lp, scen, k);
-    const double fft = a.lp.fft[pk], al = a.lp.alpha[pk], be = a.lp.beta[pk], c = cap[k];
-    const unsigned char ip = a.lp.ipow[pk];
-    const double t = bpr(fft, al, be, ip, c, x);
-    a.t[off + k] = t;
-    if (a.dtdx) a.dtdx[off + k] = bpr_dq(fft, al, be, ip, c, x);
-    write_weights(a, scen, k, t);
-    acc[0] = __dadd_rn(acc[0], __dmul_rn(x, t));
-  }
+  for (int k = blockIdx.x * kLinkBlock + threadIdx.x; k < a.m; k += gridDim.x * kLinkBlock)
+    acc[0] = __dadd_rn(acc[0], step_link(a, scen, off, cap, k, lam, tp));
   block_sum<1, kLinkBlock>(acc, sh);
   double* part = a.partials + (static_cast<size_t>(scen) * gridDim.x + blockIdx.x) * kNumSums;
   if (threadIdx.x == 0) part[0] = acc[0];
@@ -1965,25 +2018,51 @@ __global__ void __launch_bounds__(kLinkBlock) k_step(LinkArgs a) {
     double v = 0.0;
     const double* p0 = a.partials + static_cast<size_t>(scen) * gridDim.x * kNumSums;
     for (unsigned b = 0; b < gridDim.x; ++b) v = __dadd_rn(v, vload(p0 + b * kNumSums));
-    st.vht_end = v;
-    if (tape) a.lam_hist[static_cast<size_t>(scen) * a.hist_cap + it] = lam;
-    if (a.trace && it < a.trace_cap) {
-      double* r = a.trace + (static_cast<size_t>(scen) * a.trace_cap + it) * kTraceCols;
-      r[0] = st.obj;
-      r[1] = st.relgap;
-      r[2] = st.avg_excess;
-      r[3] = st.vht;
-      r[4] = lam;
-      r[5] = st.gap;
-      r[6] = it + 1;
-      r[7] = st.g0;
-    }
-    st.iter = it + 1;
-    if ((st.max_iters > 0 && st.iter >= st.max_iters) ||
-        (st.target_relgap > 0 && !(st.relgap > st.target_relgap)))
-      st.done = 1;
+    step_finish(a, scen, st, it, lam, tp, v);
     a.arrive[scen] = 0u;
   }
+}
+
+// Small networks: the whole tail of an iteration (every line-search pass,
+// the fallback, the step) by one 256-thread block per scenario, one launch
+// instead of seven; the same per-link arithmetic as k_ls_pass, k_ls_fallback
+// and k_step, with block-wide sums.
+constexpr int kTailBlock = 256;
+__global__ void __launch_bounds__(kTailBlock) k_fw_tail_small(LinkArgs a) {
+  __shared__ double sh[kNumSums * (kTailBlock / 32)];
+  __shared__ int sh_found;
+  const int scen = scen_of(a);
+  ScenState& st = a.state[scen];
+  if (st.done) return;  // (read by every thread before any change to it)
+  const size_t off = static_cast<size_t>(scen) * a.m;
+  const double* cap = a.cap + off;
+  const int passes = a.ls_mode == kLsExact ? kLsExactPasses : kLsPasses;
+  for (int pass = 0; pass < passes; ++pass) {
+    if (pass > 0 && !st.ls_pending) break;  // (uniform: written before the last barrier)
+    const int e0 = pass == 0 ? 1 : st.ls_next;
+    const double blo = pass == 0 ? 0.0 : st.ls_lo;
+    const double bhi = pass == 0 ? 1.0 : st.ls_hi;
+    double acc[kNumSums];
+#pragma unroll
+    for (int i = 0; i < kNumSums; ++i) acc[i] = 0.0;
+    for (int k = threadIdx.x; k < a.m; k += kTailBlock) ls_link(a, scen, off, cap, k, pass, e0, blo, bhi, acc);
+    block_sum<kNumSums, kTailBlock>(acc, sh);
+    if (threadIdx.x == 0)
+      ls_decide(st, acc, e0, pass, a.total_demand_s ? a.total_demand_s[scen] : a.total_demand,
+                a.ls_mode);
+    __syncthreads();
+  }
+  ls_fallback_block(a, scen, st, sh, &sh_found);
+  __syncthreads();
+  const double lam = st.lambda;
+  const int it = st.iter;
+  const TapeAt tp = tape_at(a, scen, it);
+  double acc[1] = {0.0};
+  for (int k = threadIdx.x; k < a.m; k += kTailBlock)
+    acc[0] = __dadd_rn(acc[0], step_link(a, scen, off, cap, k, lam, tp));
+  __syncthreads();  // (sh reused)
+  block_sum<1, kTailBlock>(acc, sh);
+  if (threadIdx.x == 0) step_finish(a, scen, st, it, lam, tp, acc[0]);
 }
 
 // Raise a kernel's dynamic shared-memory limit to the device maximum once, so
@@ -2188,6 +2267,11 @@ cudaError_t launch_ls_pass(const LinkArgs& a, int grid, cudaStream_t s) {
 
 cudaError_t launch_ls_fallback(const LinkArgs& a, cudaStream_t s) {
   k_ls_fallback<<<dim3(1, a.num_scen), 1024, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fw_tail_small(const LinkArgs& a, cudaStream_t s) {
+  k_fw_tail_small<<<dim3(1, a.num_scen), kTailBlock, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -179,6 +179,9 @@ cudaError_t launch_set_costs(const LinkArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_ls_pass(const LinkArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_ls_fallback(const LinkArgs& a, cudaStream_t s);
 cudaError_t launch_step(const LinkArgs& a, int grid, cudaStream_t s);
+// small networks (at most kSmallNet links): every line-search pass, the
+// fallback and the step in one launch (one block per scenario)
+cudaError_t launch_fw_tail_small(const LinkArgs& a, cudaStream_t s);
 // capacity rows [nscen][m] = base with each scenario's edits (see fw_kernels.cu)
 cudaError_t launch_scenario_caps(double* cap, const double* base, int m, int nscen, const int* ptr,
                                  const int* link, const double* val, const double* min_pos,

@@ -417,6 +417,13 @@ int Ctx::enqueue_iteration(int nscen) {
   measuring = false;
   TG_TRY(rc);
   LinkArgs la = link_args(nscen);
+  if (M <= kSmallNet) {  // small networks: the line search and the step in one launch
+    TG_TRY(mark(2, true));
+    TG_CUDA(launch_fw_tail_small(la, stream));
+    TG_TRY(mark(2, false));
+    count_launches(1);
+    return TAPGPU_OK;
+  }
   TG_TRY(mark(2, true));
   const int passes = ls_mode == kLsExact ? kLsExactPasses : kLsPasses;
   for (int p = 0; p < passes; ++p) {
