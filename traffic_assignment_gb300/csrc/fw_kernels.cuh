@@ -167,6 +167,9 @@ enum : int {
                     // chosen for networks of at most kSmallNet nodes and links)
 };
 constexpr int kSmallNet = 4096;
+// links up to which one block per scenario runs an iteration's line search
+// and step (above it the multi-block passes spread the FP64 work over SMs)
+constexpr int kSmallTail = 512;
 constexpr int kQueueSlots = 1024;  // ring slots of k_sssp_nfq
 cudaError_t launch_sssp(const PathArgs& a, bool fp64, int grid, int block, bool smem,
                         int variant, cudaStream_t s);
@@ -179,7 +182,7 @@ cudaError_t launch_set_costs(const LinkArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_ls_pass(const LinkArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_ls_fallback(const LinkArgs& a, cudaStream_t s);
 cudaError_t launch_step(const LinkArgs& a, int grid, cudaStream_t s);
-// small networks (at most kSmallNet links): every line-search pass, the
+// small networks (at most kSmallTail links): every line-search pass, the
 // fallback and the step in one launch (one block per scenario)
 cudaError_t launch_fw_tail_small(const LinkArgs& a, cudaStream_t s);
 // capacity rows [nscen][m] = base with each scenario's edits (see fw_kernels.cu)

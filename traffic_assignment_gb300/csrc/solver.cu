@@ -417,7 +417,7 @@ int Ctx::enqueue_iteration(int nscen) {
   measuring = false;
   TG_TRY(rc);
   LinkArgs la = link_args(nscen);
-  if (M <= kSmallNet) {  // small networks: the line search and the step in one launch
+  if (M <= kSmallTail) {  // small networks: the line search and the step in one launch
     TG_TRY(mark(2, true));
     TG_CUDA(launch_fw_tail_small(la, stream));
     TG_TRY(mark(2, false));
