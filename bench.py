@@ -604,8 +604,18 @@ def run_ours(args, rank, world, local_rank):
 
 def profile_case(kind):
     """A few FW iterations on the 10k-node network: every kernel of the loop
-    launches a handful of times (1,000 or 16,000 shortest-path tasks each)."""
+    launches a handful of times (1,000 or 16,000 shortest-path tasks each);
+    "small": the 416-node network (C2), one scenario, 20 iterations."""
     from traffic_assignment_gb300 import Solver, synth
+    if kind == "small":
+        net, dem = synth.make_grid416()
+        with Solver(net, dem, precision="fp32") as s:
+            r = s.solve(max_iters=20)
+            s.set_timing(True)
+            s.run_iterations(20)
+            tm = s.timing()
+        print(json.dumps({"profile_case": kind, "iterations": r["iterations"], **tm}))
+        return 0
     net, dem = synth.make_grid10k()
     with Solver(net, dem, precision="fp32") as s:
         r = s.solve(max_iters=4)
@@ -634,7 +644,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the adjoint check and the 100k-node rate")
-    ap.add_argument("--profile-case", choices=["plain", "batched"], default=None,
+    ap.add_argument("--profile-case", choices=["plain", "batched", "small"], default=None,
                     help="small case for ncu: a few FW iterations of the 10k-node network, "
                          "one scenario (plain) or 16 scenarios (batched), then exit")
     args = ap.parse_args()
