@@ -1845,9 +1845,11 @@ __device__ __forceinline__ void ls_link(const LinkArgs& a, int scen, size_t off,
 }
 
 // One line-search pass; pass 0 also forms d = y - x and the gap / objective /
-// VHT sums.  Candidates of this pass: 2^-(e0 .. e0+kLsPerPass-1).
-__global__ void __launch_bounds__(kLinkBlock) k_ls_pass(LinkArgs a) {
-  __shared__ double sh[kNumSums * (kLinkBlock / 32)];
+// VHT sums.  Candidates of this pass: 2^-(e0 .. e0+kLsPerPass-1).  BLOCK 64
+// for small networks (their FP64 work spread over more SMs), else 256.
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_ls_pass(LinkArgs a) {
+  __shared__ double sh[kNumSums * (BLOCK / 32)];
   const int scen = scen_of(a);
   ScenState& st = a.state[scen];
   if (st.done) return;
@@ -1860,9 +1862,9 @@ __global__ void __launch_bounds__(kLinkBlock) k_ls_pass(LinkArgs a) {
 #pragma unroll
   for (int i = 0; i < kNumSums; ++i) acc[i] = 0.0;
   const double* cap = a.cap + off;
-  for (int k = blockIdx.x * kLinkBlock + threadIdx.x; k < a.m; k += gridDim.x * kLinkBlock)
+  for (int k = blockIdx.x * BLOCK + threadIdx.x; k < a.m; k += gridDim.x * BLOCK)
     ls_link(a, scen, off, cap, k, a.pass, e0, blo, bhi, acc);
-  block_sum<kNumSums, kLinkBlock>(acc, sh);
+  block_sum<kNumSums, BLOCK>(acc, sh);
   double* part = a.partials + (static_cast<size_t>(scen) * gridDim.x + blockIdx.x) * kNumSums;
   if (threadIdx.x == 0) {
 #pragma unroll
@@ -1996,9 +1998,11 @@ __device__ __forceinline__ void step_finish(const LinkArgs& a, int scen, ScenSta
     st.done = 1;
 }
 
-// x += lambda d; t = BPR(x); next weights; iteration bookkeeping.
-__global__ void __launch_bounds__(kLinkBlock) k_step(LinkArgs a) {
-  __shared__ double sh[1 * (kLinkBlock / 32)];
+// x += lambda d; t = BPR(x); next weights; iteration bookkeeping (BLOCK as
+// k_ls_pass).
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_step(LinkArgs a) {
+  __shared__ double sh[1 * (BLOCK / 32)];
   const int scen = scen_of(a);
   ScenState& st = a.state[scen];
   if (st.done) return;
@@ -2008,9 +2012,9 @@ __global__ void __launch_bounds__(kLinkBlock) k_step(LinkArgs a) {
   const TapeAt tp = tape_at(a, scen, it);
   const double* cap = a.cap + off;
   double acc[1] = {0.0};
-  for (int k = blockIdx.x * kLinkBlock + threadIdx.x; k < a.m; k += gridDim.x * kLinkBlock)
+  for (int k = blockIdx.x * BLOCK + threadIdx.x; k < a.m; k += gridDim.x * BLOCK)
     acc[0] = __dadd_rn(acc[0], step_link(a, scen, off, cap, k, lam, tp));
-  block_sum<1, kLinkBlock>(acc, sh);
+  block_sum<1, BLOCK>(acc, sh);
   double* part = a.partials + (static_cast<size_t>(scen) * gridDim.x + blockIdx.x) * kNumSums;
   if (threadIdx.x == 0) part[0] = acc[0];
   if (!last_block(a.arrive + scen)) return;
@@ -2260,8 +2264,11 @@ cudaError_t launch_set_costs(const LinkArgs& a, int grid, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_ls_pass(const LinkArgs& a, int grid, cudaStream_t s) {
-  k_ls_pass<<<dim3(grid, a.num_scen), kLinkBlock, 0, s>>>(a);
+cudaError_t launch_ls_pass(const LinkArgs& a, int grid, int block, cudaStream_t s) {
+  if (block == kSmallLinkBlock)
+    k_ls_pass<kSmallLinkBlock><<<dim3(grid, a.num_scen), kSmallLinkBlock, 0, s>>>(a);
+  else
+    k_ls_pass<kLinkBlock><<<dim3(grid, a.num_scen), kLinkBlock, 0, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -2275,8 +2282,11 @@ cudaError_t launch_fw_tail_small(const LinkArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_step(const LinkArgs& a, int grid, cudaStream_t s) {
-  k_step<<<dim3(grid, a.num_scen), kLinkBlock, 0, s>>>(a);
+cudaError_t launch_step(const LinkArgs& a, int grid, int block, cudaStream_t s) {
+  if (block == kSmallLinkBlock)
+    k_step<kSmallLinkBlock><<<dim3(grid, a.num_scen), kSmallLinkBlock, 0, s>>>(a);
+  else
+    k_step<kLinkBlock><<<dim3(grid, a.num_scen), kLinkBlock, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -179,9 +179,12 @@ cudaError_t launch_aon(const PathArgs& a, bool fp64, int grid, int block, bool s
 cudaError_t launch_init_flows(const LinkArgs& a, int grid, cudaStream_t s);
 // weights = free-flow times and y_fx = 0 (first all-or-nothing)
 cudaError_t launch_set_costs(const LinkArgs& a, int grid, cudaStream_t s);
-cudaError_t launch_ls_pass(const LinkArgs& a, int grid, cudaStream_t s);
+// line-search passes and the step: `block` kSmallLinkBlock (networks of at
+// most kSmallNet links, FP64 work over more SMs) or kLinkBlock
+constexpr int kSmallLinkBlock = 64;
+cudaError_t launch_ls_pass(const LinkArgs& a, int grid, int block, cudaStream_t s);
 cudaError_t launch_ls_fallback(const LinkArgs& a, cudaStream_t s);
-cudaError_t launch_step(const LinkArgs& a, int grid, cudaStream_t s);
+cudaError_t launch_step(const LinkArgs& a, int grid, int block, cudaStream_t s);
 // small networks (at most kSmallTail links): every line-search pass, the
 // fallback and the step in one launch (one block per scenario)
 cudaError_t launch_fw_tail_small(const LinkArgs& a, cudaStream_t s);

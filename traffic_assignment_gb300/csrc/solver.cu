@@ -275,7 +275,7 @@ int Ctx::ensure_scenarios(int S) {
   }
   if (opt.record_tape) TG_TRY(alloc_n(&dtdx, sm));
   TG_TRY(alloc_n(&state, static_cast<size_t>(S)));
-  TG_TRY(alloc_n(&partials, static_cast<size_t>(S) * link_grid * kNumSums));
+  TG_TRY(alloc_n(&partials, static_cast<size_t>(S) * std::max(link_grid, ls_link_grid) * kNumSums));
   TG_TRY(alloc_n(&arrive, static_cast<size_t>(S)));
   TG_CUDA(cudaMemset(arrive, 0, sizeof(unsigned) * S));
   trace_cap = S == 1 ? 100000 : 4096;
@@ -361,6 +361,10 @@ int Ctx::plan_launches() {
     path_scratch_bytes = scratch;
   }
   link_grid = std::max(1, std::min((M + 255) / 256, 2 * num_sms));
+  // small networks: 64-thread blocks spread the line search's FP64 work
+  // over more SMs
+  ls_block = M <= kSmallNet ? kSmallLinkBlock : 256;
+  ls_link_grid = std::max(1, std::min((M + ls_block - 1) / ls_block, 2 * num_sms * (256 / ls_block)));
   return TAPGPU_OK;
 }
 
@@ -428,12 +432,12 @@ int Ctx::enqueue_iteration(int nscen) {
   const int passes = ls_mode == kLsExact ? kLsExactPasses : kLsPasses;
   for (int p = 0; p < passes; ++p) {
     la.pass = p;
-    TG_CUDA(launch_ls_pass(la, ls_grid(nscen), stream));
+    TG_CUDA(launch_ls_pass(la, ls_grid(nscen), ls_block, stream));
   }
   TG_CUDA(launch_ls_fallback(la, stream));
   TG_TRY(mark(2, false));
   TG_TRY(mark(3, true));
-  TG_CUDA(launch_step(la, link_grid, stream));
+  TG_CUDA(launch_step(la, ls_link_grid, ls_block, stream));
   TG_TRY(mark(3, false));
   count_launches(passes + 2);
   return TAPGPU_OK;
@@ -1697,11 +1701,11 @@ int tapgpu_profile_iteration(tapgpu_ctx* ctx, int reps, float* ms) {
     tapgpu::LinkArgs la = c->link_args(1);
     for (int p = 0; p < tapgpu::kLsPasses; ++p) {
       la.pass = p;
-      tapgpu::launch_ls_pass(la, c->ls_grid(1), c->stream);
+      tapgpu::launch_ls_pass(la, c->ls_grid(1), c->ls_block, c->stream);
     }
     tapgpu::launch_ls_fallback(la, c->stream);
     cudaEventRecord(ev[3], c->stream);
-    tapgpu::launch_step(la, c->link_grid, c->stream);
+    tapgpu::launch_step(la, c->ls_link_grid, c->ls_block, c->stream);
     cudaEventRecord(ev[4], c->stream);
     if (cudaEventSynchronize(ev[4]) != cudaSuccess) {
       rc = TAPGPU_ERR_CUDA;

@@ -149,6 +149,8 @@ struct Ctx {
 
   // launch shapes
   int sssp_block = 256, aon_block = 512, link_grid = 0;
+  // line-search passes and step: block size and blocks per scenario
+  int ls_block = 256, ls_link_grid = 0;
   int sssp_variant = kSsspAsync;
   double nf_delta = 1.0;      // near-far threshold step for the solver's costs
   double api_nf_delta = 1.0;  // the same for the weights of the one-shot API
@@ -159,7 +161,7 @@ struct Ctx {
   // block reductions stay a small part of the FP64 work
   int ls_grid(int nscen) const {
     const int want = (16 * num_sms + nscen - 1) / (nscen > 0 ? nscen : 1);
-    return want < 1 ? 1 : (want > link_grid ? link_grid : want);
+    return want < 1 ? 1 : (want > ls_link_grid ? ls_link_grid : want);
   }
 
   std::vector<DevMem> owned;
