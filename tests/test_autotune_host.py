@@ -14,6 +14,11 @@ def test_candidates_cover_every_variant_and_block():
     assert len(set(c)) == len(c)
     q = A.candidates(quick=True)
     assert set(q) <= set(c)
+    # small networks also try the edge-list sweeps; large ones do not
+    small, _ = synth.make_grid416()
+    big, _ = synth.make_grid10k()
+    assert "small" in {x.sssp_variant for x in A.candidates(net=small)}
+    assert "small" not in {x.sssp_variant for x in A.candidates(net=big)}
 
 
 def test_solver_kwargs():

@@ -65,12 +65,21 @@ class TuneResult:
         return self.best.solver_kwargs(net)
 
 
-def candidates(quick: bool = False) -> List[Candidate]:
-    """The sweep: every variant x block, and near-far x step scale."""
+# networks up to this many nodes and links also try the edge-list sweeps
+# (the library's default there)
+SMALL_NET = 4096
+
+
+def candidates(quick: bool = False, net: Optional[Network] = None) -> List[Candidate]:
+    """The sweep: every variant x block, and near-far x step scale; with a
+    small network (at most SMALL_NET nodes and links) the edge-list sweeps too."""
     out = []
     blocks = (256, 512) if quick else (128, 256, 512, 1024)
     scales = (8.0, 16.0, 32.0) if quick else (4.0, 8.0, 16.0, 32.0, 64.0)
-    for v in _VARIANTS:
+    variants = _VARIANTS
+    if net is not None and net.num_nodes + 1 <= SMALL_NET and net.num_links <= SMALL_NET:
+        variants = variants + ("small",)
+    for v in variants:
         for b in blocks:
             if v.startswith("nearfar"):
                 out.extend(Candidate(v, b, s, 1024) for s in scales)
@@ -154,7 +163,7 @@ def tune(net: Network, dem: Demand, precision: str = "fp32", scenarios: int = 32
     scen = scenario_list if scenario_list is not None else make_scenarios(net, scenarios,
                                                                           seed=4242)
     table = []
-    for cand in (cands if cands is not None else candidates(quick)):
+    for cand in (cands if cands is not None else candidates(quick, net)):
         try:
             row = _time_candidate(net, dem, precision, cand, scen, x0, iters, device)
         except RuntimeError as e:  # a shape that does not fit this network
