@@ -235,7 +235,10 @@ typedef struct tapgpu_options_s {
   int64_t chunk_tasks;   /* max (scenario, origin) shortest-path tasks per chunk; 0 = auto */
   int record_tape;       /* keep per-iteration flows and directions for the adjoint */
   int tape_capacity;     /* iterations kept on the tape */
-  int global_scratch;    /* 1: per-CTA labels in global memory even when shared memory fits */
+  int global_scratch;    /* 1: per-CTA labels in global memory even when shared memory fits
+                            (the queue kernels keep their bitmaps and ring in shared memory,
+                            as they do whenever the labels do not fit); 2: all per-CTA
+                            scratch in global memory */
   int sssp_variant;      /* 0 default (6 up to 4096 nodes and links, else 4, or its 32-bit
                             ring form above 65535 nodes); 1 bulk-synchronous
                             rounds; 2 asynchronous warp-owned frontier; 3 asynchronous near
@@ -249,6 +252,8 @@ typedef struct tapgpu_options_s {
                             derivative (differentiable step sizes, for the adjoint) */
   int tape_checkpoint;   /* with record_tape: flows kept every this many iterations and
                             recomputed in between by the adjoint (0 = sqrt(tape_capacity)) */
+  int sssp_ctas_per_sm;  /* resident shortest-path CTAs per SM; 0 = as many as fit */
+  int aon_ctas_per_sm;   /* resident loading CTAs per SM; 0 = as many as fit */
 } tapgpu_options;
 
 typedef struct tapgpu_result_s {

@@ -202,6 +202,33 @@ def test_bench_counts_the_scenario_state_size(tmp_path):
     assert bench.SCEN_STATE_BYTES == size
 
 
+def test_options_struct_matches_header(tmp_path):
+    """The Python front end's tapgpu_options mirror has the header's size and
+    field offsets (compiled with the C compiler against include/tap_gpu.h)."""
+    import shutil
+    import subprocess
+
+    from traffic_assignment_gb300 import _capi
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    names = [f[0] for f in _capi.Options._fields_]
+    body = "".join(f'  printf("%zu ", offsetof(tapgpu_options, {n}));\n' for n in names)
+    src = tmp_path / "opt.c"
+    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "tap_gpu.h"\n'
+                   'int main(void) {\n' + body +
+                   '  printf("%zu", sizeof(tapgpu_options));\n  return 0;\n}\n')
+    exe = tmp_path / "opt"
+    subprocess.run([cc, "-I", os.path.join(root, "include"), str(src), "-o", str(exe)],
+                   check=True, capture_output=True)
+    got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True,
+                                          text=True).stdout.split()]
+    want = [getattr(_capi.Options, n).offset for n in names] + [C.sizeof(_capi.Options)]
+    assert got == want
+
+
 # num_nodes1 (node 0 counted) whose FP64 labels and bitmaps still fit one
 # per-CTA slice of the allocation-free entry point's fixed 32 MiB array
 NOALLOC_MAX_NODES1 = 4_067_172

@@ -271,13 +271,14 @@ def test_large_network(built_lib, large_network_reference, precision):
     assert abs(ref["t"] @ y - ref["t"] @ y_ref) <= RTOL64 * (ref["t"] @ y_ref)
 
 
-@pytest.mark.parametrize("case", ["grid416", "grid3600", "grid3600_global", "grid10k_batch",
-                                  "grid416_wide_delta", "grid416_narrow_delta"])
+@pytest.mark.parametrize("case", ["grid416", "grid3600", "grid3600_global", "grid3600_allglobal",
+                                  "grid10k_batch", "grid416_wide_delta", "grid416_narrow_delta"])
 def test_queue_kernel_equals_near_far_kernel(built_lib, case):
     """The queue kernel (its far set read off the labels at each phase step)
     and the bitmap near-far kernel reach the same least fixed point of the
     FP32 relaxations, so labels, trees and flows are bit-identical: single
-    scenarios, labels in global memory, a batch of warm-started scenarios, and
+    scenarios, labels in global memory (with the ring and bitmaps in shared or
+    in global memory), a batch of warm-started scenarios, and
     threshold steps so wide that the whole graph is one near set (the ring
     overflows into the bitmap) or so narrow that most phases hold few nodes."""
     kw = {}
@@ -285,7 +286,9 @@ def test_queue_kernel_equals_near_far_kernel(built_lib, case):
         net, dem = synth.make_grid416()
     elif case.startswith("grid3600"):
         net, dem = synth.make_grid3600()
-        kw["global_scratch"] = case.endswith("global")
+        # labels in global memory: with the queue's ring and bitmaps in shared
+        # memory, or all of it in global memory
+        kw["global_scratch"] = 2 if case.endswith("allglobal") else int(case.endswith("global"))
     else:
         net, dem = synth.make_grid10k()
     if case == "grid416_wide_delta":

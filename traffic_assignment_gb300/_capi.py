@@ -47,7 +47,8 @@ class Options(C.Structure):
                 ("chunk_tasks", C.c_int64), ("record_tape", C.c_int),
                 ("tape_capacity", C.c_int), ("global_scratch", C.c_int),
                 ("sssp_variant", C.c_int), ("nf_delta", C.c_double),
-                ("line_search", C.c_int), ("tape_checkpoint", C.c_int)]
+                ("line_search", C.c_int), ("tape_checkpoint", C.c_int),
+                ("sssp_ctas_per_sm", C.c_int), ("aon_ctas_per_sm", C.c_int)]
 
 
 class Result(C.Structure):

@@ -958,9 +958,13 @@ __device__ __forceinline__ void nfq_expand(const PathArgs& a, const uint2* e4s, 
 }
 
 // five 256-thread CTAs per SM fit the shared memory of a 10k-node network:
-// keep registers to that occupancy
-template <typename T, int BLOCK, bool SMEM, typename R>
+// keep registers to that occupancy.  SPLIT (labels too large for shared
+// memory): the labels live in the CTA's global scratch slice, the near/far
+// bitmaps and the ring in shared memory, so that only the label atomics go
+// to L2.
+template <typename T, int BLOCK, bool SMEM, typename R, bool SPLIT = false>
 __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) k_sssp_nfq(PathArgs a) {
+  static_assert(!(SMEM && SPLIT), "the split layout keeps the labels in global memory");
   using U = typename DT<T>::U;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int sh_task;
@@ -974,7 +978,7 @@ __global__ void __launch_bounds__(BLOCK, (1280 / BLOCK > 0 ? 1280 / BLOCK : 1)) 
       SMEM ? smem_raw
            : static_cast<unsigned char*>(a.scratch) + static_cast<size_t>(blockIdx.x) * a.scratch_stride;
   U* dist = reinterpret_cast<U*>(base);
-  unsigned* near = reinterpret_cast<unsigned*>(base + align16(sizeof(U) * n1));
+  unsigned* near = reinterpret_cast<unsigned*>(SPLIT ? smem_raw : base + align16(sizeof(U) * n1));
   unsigned* far = near + nwords;
   R* ring = reinterpret_cast<R*>(far + nwords);
   const int lane = threadIdx.x & 31;
@@ -2106,8 +2110,21 @@ PathKernel sssp_kernel(int variant) {
   return k_sssp_nf<T, BLOCK, SMEM>;
 }
 
+template <typename T, int BLOCK>
+PathKernel nfq_split_kernel(int variant) {
+  return variant == kSsspNearFarQueue ? k_sssp_nfq<T, BLOCK, false, unsigned short, true>
+                                      : k_sssp_nfq<T, BLOCK, false, unsigned, true>;
+}
+
 template <typename T, int BLOCK, bool SMEM>
 cudaError_t launch_sssp_t(const PathArgs& a, int grid, size_t smem, int variant, cudaStream_t s) {
+  if (!SMEM && !a.all_global && nfq_split(a.g.n1, variant)) {
+    PathKernel fn = nfq_split_kernel<T, BLOCK>(variant);
+    cudaError_t e = allow_max_smem(fn);
+    if (e != cudaSuccess) return e;
+    fn<<<grid, BLOCK, nfq_split_smem_bytes(a.g.n1, variant), s>>>(a);
+    return cudaGetLastError();
+  }
   PathKernel fn = sssp_kernel<T, BLOCK, SMEM>(variant);
   if (SMEM) {
     cudaError_t e = allow_max_smem(fn);
@@ -2139,6 +2156,19 @@ size_t sssp_smem_bytes(int n1, bool fp64, int variant, int m) {
                       : variant == kSsspNearFarQueueWide ? sizeof(unsigned) * kQCap
                                                          : 0;
   return align16(align16((fp64 ? 8 : 4) * static_cast<size_t>(n1)) + 2 * 4 * words + ring);
+}
+
+size_t nfq_split_smem_bytes(int n1, int variant) {
+  const size_t words = (static_cast<size_t>(n1) + 31) / 32;
+  const size_t ring =
+      variant == kSsspNearFarQueue ? sizeof(unsigned short) * kQCap : sizeof(unsigned) * kQCap;
+  return align16(2 * 4 * words + ring);
+}
+
+// (200 KB of bitmaps: networks up to ~6.5 million nodes)
+bool nfq_split(int n1, int variant) {
+  return (variant == kSsspNearFarQueue || variant == kSsspNearFarQueueWide) &&
+         nfq_split_smem_bytes(n1, variant) <= (size_t(200) << 10);
 }
 
 // Both sizes are also the stride between CTAs' slices of the global-memory
@@ -2199,8 +2229,16 @@ cudaError_t launch_aon(const PathArgs& a, bool fp64, int grid, int block, bool s
 }
 
 template <typename T, int BLOCK, bool SMEM>
-int occ_sssp_t(size_t smem, int variant) {
+int occ_sssp_t(size_t smem, int variant, int n1, bool all_global) {
   PathKernel fn = sssp_kernel<T, BLOCK, SMEM>(variant);
+  if (!SMEM && !all_global && nfq_split(n1, variant)) {
+    fn = nfq_split_kernel<T, BLOCK>(variant);
+    smem = nfq_split_smem_bytes(n1, variant);
+    if (allow_max_smem(fn) != cudaSuccess) return 0;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, BLOCK, smem) != cudaSuccess) return 0;
+    return n;
+  }
   if (SMEM && allow_max_smem(fn) != cudaSuccess) return 0;
   int n = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, BLOCK, SMEM ? smem : 0) != cudaSuccess)
@@ -2218,14 +2256,14 @@ int occ_aon_t(size_t smem) {
   return n;
 }
 
-int sssp_occupancy(bool fp64, int block, bool smem, int n1, int variant, int m) {
+int sssp_occupancy(bool fp64, int block, bool smem, int n1, int variant, int m, bool all_global) {
   const size_t bytes = sssp_smem_bytes(n1, fp64, variant, m);
-#define TAPGPU_OCC(B)                                                                     \
-  if (block == B) {                                                                       \
-    if (fp64) return smem ? occ_sssp_t<double, B, true>(bytes, variant)                   \
-                          : occ_sssp_t<double, B, false>(bytes, variant);                 \
-    return smem ? occ_sssp_t<float, B, true>(bytes, variant)                              \
-                : occ_sssp_t<float, B, false>(bytes, variant);                            \
+#define TAPGPU_OCC(B)                                                                       \
+  if (block == B) {                                                                         \
+    if (fp64) return smem ? occ_sssp_t<double, B, true>(bytes, variant, n1, all_global)     \
+                          : occ_sssp_t<double, B, false>(bytes, variant, n1, all_global);   \
+    return smem ? occ_sssp_t<float, B, true>(bytes, variant, n1, all_global)                \
+                : occ_sssp_t<float, B, false>(bytes, variant, n1, all_global);              \
   }
   TAPGPU_OCC(128)
   TAPGPU_OCC(256)

@@ -103,6 +103,7 @@ struct PathArgs {
   int do_load;                  // 0: predecessors only
   void* scratch;                // per-CTA global scratch when the smem variant does not fit
   long long scratch_stride;     // bytes per CTA
+  int all_global;               // global scratch: the queue kernels' bitmaps and ring too
   unsigned long long* stats;    // optional [4]: rounds, tasks, node expansions, -
   double nf_delta;              // near-far threshold step (label units)
 };
@@ -153,6 +154,10 @@ struct LinkArgs {
 // launch helpers (implemented in fw_kernels.cu)
 // (m: links, used by the small-network variant, whose edge list is held too)
 size_t sssp_smem_bytes(int n1, bool fp64, int variant = 0, int m = 0);
+// The queue kernels with labels in global memory keep their near/far bitmaps
+// and ring in shared memory (these bytes) while they fit.
+size_t nfq_split_smem_bytes(int n1, int variant);
+bool nfq_split(int n1, int variant);
 size_t aon_smem_bytes(int n1, bool fp64);
 bool aon_compact(int n1, bool fp64);  // 10-byte-per-node loading layout
 int max_smem_optin(int device);
@@ -200,8 +205,8 @@ cudaError_t launch_param_rows(unsigned char* rows, const unsigned char* base, in
                               cudaStream_t s);
 // rows 1 .. nscen-1 of x [nscen][m] become copies of row 0
 cudaError_t launch_replicate_rows(double* x, int m, int nscen, int grid, cudaStream_t s);
-int sssp_occupancy(bool fp64, int block, bool smem, int n1, int variant,
-                   int m = 0);  // CTAs per SM
+int sssp_occupancy(bool fp64, int block, bool smem, int n1, int variant, int m = 0,
+                   bool all_global = false);  // CTAs per SM
 int aon_occupancy(bool fp64, int block, bool smem, int n1);
 
 }  // namespace tapgpu

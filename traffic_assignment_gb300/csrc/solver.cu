@@ -187,6 +187,7 @@ PathArgs Ctx::path_args(int nscen_slots) const {
   a.do_load = 1;
   a.scratch = path_scratch;
   a.scratch_stride = 0;
+  a.all_global = opt.global_scratch == 2;
   a.stats = timing ? path_stats : nullptr;
   a.nf_delta = nf_delta;
   a.e4 = (!fp64 && (sssp_variant == kSsspNearFarQueue || sssp_variant == kSsspNearFarQueueWide))
@@ -345,12 +346,14 @@ int Ctx::plan_launches() {
   const size_t room = optin > 1024 ? static_cast<size_t>(optin - 1024) : 0;
   sssp_smem = sssp_smem_bytes(n1, fp64, sssp_variant, M) <= room && !opt.global_scratch;
   aon_smem = aon_smem_bytes(n1, fp64) <= room && !opt.global_scratch;
-  int so = sssp_occupancy(fp64, sssp_block, sssp_smem, n1, sssp_variant, M);
+  int so = sssp_occupancy(fp64, sssp_block, sssp_smem, n1, sssp_variant, M, opt.global_scratch == 2);
   int ao = aon_occupancy(fp64, aon_block, aon_smem, n1);
   if (so <= 0 || ao <= 0) {
     set_message("no resident CTA fits for the shortest-path kernels");
     return TAPGPU_ERR_UNSUPPORTED;
   }
+  if (opt.sssp_ctas_per_sm > 0) so = std::min(so, opt.sssp_ctas_per_sm);
+  if (opt.aon_ctas_per_sm > 0) ao = std::min(ao, opt.aon_ctas_per_sm);
   sssp_grid = so * num_sms;
   aon_grid = ao * num_sms;
   size_t scratch = 0;
@@ -1490,7 +1493,8 @@ int tapgpu_sssp(tapgpu_ctx* ctx, const double* weights, const int64_t* srcs, int
     a.nf_delta = c->api_nf_delta;
     const int optin = tapgpu::max_smem_optin(c->device);
     const bool s_smem = tapgpu::sssp_smem_bytes(n1, true, c->sssp_variant, c->M) + 1024 <= static_cast<size_t>(optin);
-    const int occ = tapgpu::sssp_occupancy(true, c->sssp_block, s_smem, n1, c->sssp_variant, c->M);
+    const int occ = tapgpu::sssp_occupancy(true, c->sssp_block, s_smem, n1, c->sssp_variant, c->M,
+                                           c->opt.global_scratch == 2);
     int grid = std::max(1, std::min(occ * c->num_sms, ns));
     if (!s_smem) {
       const size_t need = tapgpu::sssp_smem_bytes(n1, true, c->sssp_variant, c->M) * static_cast<size_t>(grid);

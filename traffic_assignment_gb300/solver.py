@@ -57,9 +57,10 @@ class Solver:
                  device: int = 0, sssp_block: int = 0, aon_block: int = 0,
                  iters_per_launch: int = 0, use_graphs: bool = True, chunk_tasks: int = 0,
                  record_tape: bool = False, tape_capacity: int = 0,
-                 global_scratch: bool = False, sssp_variant: str = "default",
+                 global_scratch: int = 0, sssp_variant: str = "default",
                  nf_delta: float = 0.0, line_search: str = "reference",
-                 tape_checkpoint: int = 0):
+                 tape_checkpoint: int = 0, sssp_ctas_per_sm: int = 0,
+                 aon_ctas_per_sm: int = 0):
         self.L = K.load()
         self.net = net
         self.dem = dem
@@ -74,12 +75,15 @@ class Solver:
         opt.chunk_tasks = chunk_tasks
         opt.record_tape = 1 if record_tape else 0
         opt.tape_capacity = tape_capacity
-        opt.global_scratch = 1 if global_scratch else 0
+        # True / 1: labels in global memory; 2: the queue kernels' bitmaps and ring too
+        opt.global_scratch = int(global_scratch)
         opt.sssp_variant = {"default": 0, "rounds": 1, "async": 2, "nearfar": 3,
                             "nearfar_queue": 4, "small": 6}[sssp_variant]
         opt.nf_delta = float(nf_delta)
         opt.line_search = {"reference": 0, "exact": 1}[line_search]
         opt.tape_checkpoint = int(tape_checkpoint)
+        opt.sssp_ctas_per_sm = int(sssp_ctas_per_sm)
+        opt.aon_ctas_per_sm = int(aon_ctas_per_sm)
         self.precision = "fp32" if opt.precision == K.TAPGPU_FP32_PATHS else "fp64"
         self.last_scenarios = 1
         keep: list = []
