@@ -605,8 +605,18 @@ def run_ours(args, rank, world, local_rank):
 def profile_case(kind):
     """A few FW iterations on the 10k-node network: every kernel of the loop
     launches a handful of times (1,000 or 16,000 shortest-path tasks each);
-    "small": the 416-node network (C2), one scenario, 20 iterations."""
+    "small": the 416-node network (C2), one scenario, 20 iterations;
+    "large": the 100k-node network (C5), one scenario, 3 iterations (4,000
+    tasks per launch, labels in global memory)."""
     from traffic_assignment_gb300 import Solver, synth
+    if kind == "large":
+        net, dem = synth.make_grid100k()
+        with Solver(net, dem, precision="fp32") as s:
+            s.set_timing(True)
+            r = s.solve(max_iters=3)
+            tm = s.timing()
+        print(json.dumps({"profile_case": kind, "iterations": r["iterations"], **tm}))
+        return 0
     if kind == "small":
         net, dem = synth.make_grid416()
         with Solver(net, dem, precision="fp32") as s:
@@ -644,9 +654,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the adjoint check and the 100k-node rate")
-    ap.add_argument("--profile-case", choices=["plain", "batched", "small"], default=None,
+    ap.add_argument("--profile-case", choices=["plain", "batched", "small", "large"],
+                    default=None,
                     help="small case for ncu: a few FW iterations of the 10k-node network, "
-                         "one scenario (plain) or 16 scenarios (batched), then exit")
+                         "one scenario (plain) or 16 scenarios (batched), of the 416-node "
+                         "network (small) or of the 100k-node network (large), then exit")
     args = ap.parse_args()
     rank, world, local_rank = _env_rank()
     if args.profile_case:

@@ -1412,15 +1412,31 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
     }
     __syncthreads();
     int pend = 0;
-    for (int v = threadIdx.x; v < n1; v += BLOCK) {
-      unsigned p = up[v];
-      if (v == src || DT<T>::bits(dS[v]) == DT<T>::kInf) {
-        p = kPredRoot;
-      } else if (p == kPredNone) {
-        p = kPredPending;
-        pend = 1;
+    {
+      auto settle = [&](int v, unsigned p, T d) {
+        if (v == src || DT<T>::bits(d) == DT<T>::kInf) {
+          p = kPredRoot;
+        } else if (p == kPredNone) {
+          p = kPredPending;
+          pend = 1;
+        }
+        up[v] = p;
+      };
+      int v = threadIdx.x;
+      if constexpr (!SMEM) {  // global layout: four nodes' words and labels in flight
+        for (; v + 3 * BLOCK < n1; v += 4 * BLOCK) {
+          unsigned p[4];
+          T d[4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            p[j] = up[v + j * BLOCK];
+            d[j] = dS[v + j * BLOCK];
+          }
+#pragma unroll
+          for (int j = 0; j < 4; ++j) settle(v + j * BLOCK, p[j], d[j]);
+        }
       }
-      up[v] = p;
+      for (; v < n1; v += BLOCK) settle(v, up[v], dS[v]);
     }
     pend = __syncthreads_or(pend);
     // Rare: labels reached only over links too short to change them (zero or
@@ -1467,14 +1483,29 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
       }
     }
     __syncthreads();  // (COMPACT: the scratch reads of the loop above precede the links' writes)
-    for (int v = threadIdx.x; v < n1; v += BLOCK) {
-      const unsigned p = up[v];
-      const bool ok = p < kPredRoot;
-      if constexpr (COMPACT) {
-        par16[v] = ok ? static_cast<unsigned short>(pack ? (p & 0xffffu) : __ldg(a.g.tail + p))
-                      : kNoParent16;
-      } else {
-        parent[v] = ok ? __ldg(a.g.tail + p) : -1;
+    {
+      int v = threadIdx.x;
+      if constexpr (!SMEM && !COMPACT) {  // four nodes' words, then their tails, in flight
+        for (; v + 3 * BLOCK < n1; v += 4 * BLOCK) {
+          unsigned p[4];
+          int u[4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) p[j] = up[v + j * BLOCK];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) u[j] = p[j] < kPredRoot ? __ldg(a.g.tail + p[j]) : -1;
+#pragma unroll
+          for (int j = 0; j < 4; ++j) parent[v + j * BLOCK] = u[j];
+        }
+      }
+      for (; v < n1; v += BLOCK) {
+        const unsigned p = up[v];
+        const bool ok = p < kPredRoot;
+        if constexpr (COMPACT) {
+          par16[v] = ok ? static_cast<unsigned short>(pack ? (p & 0xffffu) : __ldg(a.g.tail + p))
+                        : kNoParent16;
+        } else {
+          parent[v] = ok ? __ldg(a.g.tail + p) : -1;
+        }
       }
     }
     if (a.pred_out) {
@@ -1563,7 +1594,28 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
     }
     __syncthreads();
     unsigned long long* y = a.y_fx + static_cast<size_t>(scen) * a.g.m;
-    for (int v = threadIdx.x; v < n1; v += BLOCK) {
+    int vf = threadIdx.x;
+    if constexpr (!SMEM) {  // global layout: four nodes' totals and links in flight
+      for (; vf + 3 * BLOCK < n1; vf += 4 * BLOCK) {
+        unsigned long long q[4];
+        unsigned k[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int v = vf + j * BLOCK;
+          if constexpr (kWalk32) {
+            q[j] = static_cast<unsigned long long>(tot32[v]) << kshift;
+            k[j] = COMPACT && pack ? up[v] >> 16 : up[v];
+          } else {
+            q[j] = static_cast<unsigned long long>(thr[v]);
+            k[j] = static_cast<unsigned>(pred[v]);
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (q[j] != 0ull) atomicAdd(y + k[j], q[j]);
+      }
+    }
+    for (int v = vf; v < n1; v += BLOCK) {
       if constexpr (kWalk32) {
         // the 32-bit totals cover the labels only: the predecessor words
         // (the link, packed with the tail in the compact layout) are intact
