@@ -1377,66 +1377,118 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
     // no lookup of the link's tail; the minimum still orders by link.
     const bool pack = COMPACT && a.g.m <= 0xffff;
     unsigned* up = reinterpret_cast<unsigned*>(pred);
-    for (int v = threadIdx.x; v < n1; v += BLOCK) up[v] = kPredNone;
-    __syncthreads();
-
-    // Predecessor = lowest-numbered tight in-link from a strictly closer tail:
-    // one sweep over the reverse-star slots (contiguous records, in link order
-    // within a node), keeping the smallest tight link of each head.
-    {
-      const int m = a.g.m;
-      for (int i0 = threadIdx.x; i0 < m; i0 += kEdgeGroup * BLOCK) {
-        int vv[kEdgeGroup], uu[kEdgeGroup];
-        T ww[kEdgeGroup];
+    int pend = 0;
+    bool by_node = false;
+    if constexpr (COMPACT) {
+      if (pack && a.r4) {
+        // The same predecessors, node by node: each node's first four
+        // in-links come from one padded 32-byte block of {link << 16 | tail,
+        // weight} records (in link order; the first word is the predecessor
+        // word itself), further in-links from the reverse-star records; the
+        // first tight one is the lowest-numbered, so each node's word is
+        // written once, without atomics, and the settling of roots and
+        // pending nodes happens in the same pass.
+        by_node = true;
+        __syncthreads();  // (labels in)
+        const uint4* r4s = reinterpret_cast<const uint4*>(a.r4 + static_cast<size_t>(scen) * n1 * 4);
+        for (int v = threadIdx.x; v < n1; v += BLOCK) {
+          const T dv = dS[v];
+          unsigned p = kPredRoot;
+          if (v != src && DT<T>::bits(dv) != DT<T>::kInf) {
+            p = kPredNone;
+            const int i0 = __ldg(a.g.in_ptr + v), deg = __ldg(a.g.in_ptr + v + 1) - i0;
+            const uint4 q0 = __ldg(r4s + 2 * v), q1 = __ldg(r4s + 2 * v + 1);
+            const unsigned wx[4] = {q0.x, q0.z, q1.x, q1.z};
+            const unsigned wb[4] = {q0.y, q0.w, q1.y, q1.w};
 #pragma unroll
-        for (int j = 0; j < kEdgeGroup; ++j) {
-          const int i = i0 + j * BLOCK;
-          vv[j] = -1;
-          uu[j] = 0;
-          if (i < m) {
-            vv[j] = __ldg(a.g.in_head + i);
-            rv.load(i, uu[j], ww[j]);
+            for (int j = 0; j < 4; ++j) {
+              if (p == kPredNone && j < deg) {
+                const int u = static_cast<int>(wx[j] & 0xffffu);
+                if (!(u < F && u != src)) {
+                  const T du = dS[u];
+                  if (du < dv && DT<T>::add(du, __uint_as_float(wb[j])) == dv) p = wx[j];
+                }
+              }
+            }
+            for (int i = i0 + 4; p == kPredNone && i < i0 + deg; ++i) {
+              int u;
+              T w;
+              rv.load(i, u, w);
+              if (u < F && u != src) continue;
+              const T du = dS[u];
+              if (du < dv && DT<T>::add(du, w) == dv)
+                p = (static_cast<unsigned>(rv.link(i)) << 16) | static_cast<unsigned>(u);
+            }
+            if (p == kPredNone) {
+              p = kPredPending;
+              pend = 1;
+            }
           }
-        }
-#pragma unroll
-        for (int j = 0; j < kEdgeGroup; ++j) {
-          const int v = vv[j], u = uu[j];
-          if (v < 0 || v == src || (u < F && u != src)) continue;
-          const T dv = dS[v], du = dS[u];
-          if (du < dv && DT<T>::add(du, ww[j]) == dv) {
-            const unsigned k = static_cast<unsigned>(rv.link(i0 + j * BLOCK));
-            atomicMin(up + v, pack ? (k << 16) | static_cast<unsigned>(u) : k);
-          }
+          up[v] = p;
         }
       }
     }
-    __syncthreads();
-    int pend = 0;
-    {
-      auto settle = [&](int v, unsigned p, T d) {
-        if (v == src || DT<T>::bits(d) == DT<T>::kInf) {
-          p = kPredRoot;
-        } else if (p == kPredNone) {
-          p = kPredPending;
-          pend = 1;
-        }
-        up[v] = p;
-      };
-      int v = threadIdx.x;
-      if constexpr (!SMEM) {  // global layout: four nodes' words and labels in flight
-        for (; v + 3 * BLOCK < n1; v += 4 * BLOCK) {
-          unsigned p[4];
-          T d[4];
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            p[j] = up[v + j * BLOCK];
-            d[j] = dS[v + j * BLOCK];
+    if (!by_node) {
+      for (int v = threadIdx.x; v < n1; v += BLOCK) up[v] = kPredNone;
+      __syncthreads();
+
+      // Predecessor = lowest-numbered tight in-link from a strictly closer tail:
+      // one sweep over the reverse-star slots (contiguous records, in link order
+      // within a node), keeping the smallest tight link of each head.
+      {
+        const int m = a.g.m;
+        for (int i0 = threadIdx.x; i0 < m; i0 += kEdgeGroup * BLOCK) {
+          int vv[kEdgeGroup], uu[kEdgeGroup];
+          T ww[kEdgeGroup];
+  #pragma unroll
+          for (int j = 0; j < kEdgeGroup; ++j) {
+            const int i = i0 + j * BLOCK;
+            vv[j] = -1;
+            uu[j] = 0;
+            if (i < m) {
+              vv[j] = __ldg(a.g.in_head + i);
+              rv.load(i, uu[j], ww[j]);
+            }
           }
-#pragma unroll
-          for (int j = 0; j < 4; ++j) settle(v + j * BLOCK, p[j], d[j]);
+  #pragma unroll
+          for (int j = 0; j < kEdgeGroup; ++j) {
+            const int v = vv[j], u = uu[j];
+            if (v < 0 || v == src || (u < F && u != src)) continue;
+            const T dv = dS[v], du = dS[u];
+            if (du < dv && DT<T>::add(du, ww[j]) == dv) {
+              const unsigned k = static_cast<unsigned>(rv.link(i0 + j * BLOCK));
+              atomicMin(up + v, pack ? (k << 16) | static_cast<unsigned>(u) : k);
+            }
+          }
         }
       }
-      for (; v < n1; v += BLOCK) settle(v, up[v], dS[v]);
+      __syncthreads();
+      {
+        auto settle = [&](int v, unsigned p, T d) {
+          if (v == src || DT<T>::bits(d) == DT<T>::kInf) {
+            p = kPredRoot;
+          } else if (p == kPredNone) {
+            p = kPredPending;
+            pend = 1;
+          }
+          up[v] = p;
+        };
+        int v = threadIdx.x;
+        if constexpr (!SMEM) {  // global layout: four nodes' words and labels in flight
+          for (; v + 3 * BLOCK < n1; v += 4 * BLOCK) {
+            unsigned p[4];
+            T d[4];
+  #pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              p[j] = up[v + j * BLOCK];
+              d[j] = dS[v + j * BLOCK];
+            }
+  #pragma unroll
+            for (int j = 0; j < 4; ++j) settle(v + j * BLOCK, p[j], d[j]);
+          }
+        }
+        for (; v < n1; v += BLOCK) settle(v, up[v], dS[v]);
+      }
     }
     pend = __syncthreads_or(pend);
     // Rare: labels reached only over links too short to change them (zero or
@@ -1719,6 +1771,10 @@ __device__ __forceinline__ void write_weights(const LinkArgs& a, int scen, int k
     if (a.e4) {
       const int p = __ldg(a.ell_pos + k);
       if (p >= 0) a.e4[static_cast<size_t>(scen) * a.n1 * 4 + p] = make_uint2(__ldg(a.e4x + k), bits);
+    }
+    if (a.r4) {
+      const int p = __ldg(a.r4_pos + k);
+      if (p >= 0) a.r4[static_cast<size_t>(scen) * a.n1 * 4 + p] = make_uint2(__ldg(a.r4x + k), bits);
     }
   }
   if (a.w64) a.w64[i] = t;

@@ -84,6 +84,8 @@ struct PathArgs {
   const uint2* e32;             // [S][m] {head, f32 weight bits} when fp32 paths
   const uint2* e4;              // [S][n1][4] the first four records of each node, or nullptr
   const uint2* r32;             // [S][m] {tail, f32 weight bits} in reverse-star order
+  const uint2* r4;              // [S][n1][4] the first four in-link records of each node
+                                //     {link << 16 | tail, f32 weight bits}, or nullptr
   const double* w64;            // [S][m] when fp64 paths
   const int* sources;           // source nodes
   int num_sources;
@@ -125,6 +127,9 @@ struct LinkArgs {
                                 //     tail's out-degree in the upper 16 bits (16-bit queue ring)
   int n1;
   uint2* r32;                   // [S][m] packed fp32 reverse records (with e32)
+  uint2* r4;                    // [S][n1][4] first four in-link records of each node, or nullptr
+  const int* r4_pos;            // [m] slot of link k among its head's four (-1: beyond the fourth)
+  const unsigned* r4x;          // [m] first word of link k's padded reverse record
   const int* head;              // [m] head node of each link (for e32)
   const int* tail;              // [m] tail node of each link (for r32)
   const int* rpos;              // [m] reverse-star slot of each link (for r32)

@@ -193,6 +193,7 @@ PathArgs Ctx::path_args(int nscen_slots) const {
   a.e4 = (!fp64 && (sssp_variant == kSsspNearFarQueue || sssp_variant == kSsspNearFarQueueWide))
              ? e4
              : nullptr;
+  a.r4 = rev4 ? r4 : nullptr;
   return a;
 }
 
@@ -213,6 +214,9 @@ LinkArgs Ctx::link_args(int nscen) const {
   a.e4 = fp64 ? nullptr : e4;
   a.ell_pos = ell_pos;
   a.e4x = e4x;
+  a.r4 = rev4 && !fp64 ? r4 : nullptr;
+  a.r4_pos = r4_pos;
+  a.r4x = r4x;
   a.n1 = n1;
   a.head = head;
   a.tail = tail;
@@ -243,13 +247,14 @@ LinkArgs Ctx::link_args(int nscen) const {
 int Ctx::ensure_scenarios(int S) {
   if (S <= S_cap) return TAPGPU_OK;
   // release the old per-scenario arrays
-  void* olds[] = {cap, x, t, d, dtdx, yfx, e32, r32, e4, w64, state, partials, arrive, trace, scen_list,
-                  x_hist, d_hist, lam_hist};
+  void* olds[] = {cap, x, t, d, dtdx, yfx, e32, r32, e4, r4, w64, state, partials, arrive, trace,
+                  scen_list, x_hist, d_hist, lam_hist};
   for (void* p : olds) free_owned(this, p);
   cap = x = t = d = dtdx = nullptr;
   yfx = nullptr;
   e32 = nullptr;
   e4 = nullptr;
+  r4 = nullptr;
   r32 = nullptr;
   w64 = nullptr;
   state = nullptr;
@@ -273,6 +278,10 @@ int Ctx::ensure_scenarios(int S) {
     const size_t s4 = static_cast<size_t>(S) * n1 * 4;
     TG_TRY(alloc_n(&e4, s4));
     TG_CUDA(cudaMemset(e4, 0, sizeof(uint2) * s4));
+    if (rev4) {
+      TG_TRY(alloc_n(&r4, s4));
+      TG_CUDA(cudaMemset(r4, 0, sizeof(uint2) * s4));
+    }
   }
   if (opt.record_tape) TG_TRY(alloc_n(&dtdx, sm));
   TG_TRY(alloc_n(&state, static_cast<size_t>(S)));
@@ -380,6 +389,7 @@ int Ctx::enqueue_paths(int nscen, bool load, const uint2* e32p, const uint2* r32
     if (a.e4) a.e4 = e32p == e32 ? e4 : (e32p == api_e32 ? api_e4 : nullptr);
     a.e32 = e32p;
     a.r32 = r32p;
+    if (r32p != r32) a.r4 = nullptr;  // (the padded reverse records follow the context's own)
     a.w64 = w64p;
     a.y_fx = ydst;
     a.do_load = load ? 1 : 0;
@@ -723,6 +733,20 @@ static int create_impl(const tapgpu_network* net, const tapgpu_demand* dem,
     }
     TG_CUDA(cudaMemcpy(c->out_deg, deg.data(), sizeof(int) * n1, cudaMemcpyHostToDevice));
     TG_CUDA(cudaMemcpy(c->ell_pos, pos.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
+    c->rev4 = !c->fp64 && n1 <= 0xffff && M <= 0xffff;
+    if (c->rev4) {
+      std::vector<int> rpos4(M);
+      std::vector<unsigned> rx(M);
+      for (int k = 0; k < M; ++k) {
+        const int v = c->h_head[k], j = c->h_rpos[k] - ip_in[v];
+        rpos4[k] = j < 4 ? v * 4 + j : -1;
+        rx[k] = (static_cast<unsigned>(k) << 16) | static_cast<unsigned>(c->h_tail[k]);
+      }
+      TG_TRY(c->alloc_n(&c->r4_pos, M));
+      TG_TRY(c->alloc_n(&c->r4x, M));
+      TG_CUDA(cudaMemcpy(c->r4_pos, rpos4.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
+      TG_CUDA(cudaMemcpy(c->r4x, rx.data(), sizeof(unsigned) * M, cudaMemcpyHostToDevice));
+    }
     TG_CUDA(cudaMemcpy(c->e4x, c->h_e4x.data(), sizeof(unsigned) * M, cudaMemcpyHostToDevice));
   }
   TG_CUDA(cudaMemcpy(c->rpos, c->h_rpos.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
@@ -1487,6 +1511,7 @@ int tapgpu_sssp(tapgpu_ctx* ctx, const double* weights, const int64_t* srcs, int
     a.task_end = ns;
     a.w64 = c->api_w64;
     a.e32 = nullptr;
+    a.r4 = nullptr;
     a.do_load = 0;
     a.pred_out = c->pred_buf;
     a.y_fx = c->api_yfx;

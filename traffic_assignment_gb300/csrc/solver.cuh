@@ -49,6 +49,11 @@ struct Ctx {
   std::vector<unsigned> h_e4x;
   bool deg16 = false;       // node ids and out-degrees fit 16 bits (16-bit queue ring)
   std::vector<int> h_ell_pos;
+  // padded reverse records of the loading kernel's per-node predecessor scan
+  // (FP32 paths, nodes and links fitting 16 bits)
+  bool rev4 = false;
+  int* r4_pos = nullptr;    // slot of each link among its head's first four in-links (-1: beyond)
+  unsigned* r4x = nullptr;  // first word of each link's padded reverse record (link << 16 | tail)
   double *fft = nullptr, *alpha = nullptr, *beta = nullptr;
   unsigned char* ipow = nullptr;
 
@@ -84,6 +89,7 @@ struct Ctx {
   uint2* e32 = nullptr;  // packed {head, f32 weight} per scenario and link
   uint2* r32 = nullptr;  // packed {tail, f32 weight} per scenario, reverse-star order
   uint2* e4 = nullptr;   // per scenario, the first four records of each node (padded)
+  uint2* r4 = nullptr;   // per scenario, the first four in-link records of each node (padded)
   int* rpos = nullptr;   // reverse-star slot of each link
   std::vector<int> h_rpos;
   double* w64 = nullptr;
