@@ -1391,26 +1391,24 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
         by_node = true;
         __syncthreads();  // (labels in)
         const uint4* r4s = reinterpret_cast<const uint4*>(a.r4 + static_cast<size_t>(scen) * n1 * 4);
-        for (int v = threadIdx.x; v < n1; v += BLOCK) {
-          const T dv = dS[v];
-          unsigned p = kPredRoot;
-          if (v != src && DT<T>::bits(dv) != DT<T>::kInf) {
-            p = kPredNone;
-            const int i0 = __ldg(a.g.in_ptr + v), deg = __ldg(a.g.in_ptr + v + 1) - i0;
-            const uint4 q0 = __ldg(r4s + 2 * v), q1 = __ldg(r4s + 2 * v + 1);
-            const unsigned wx[4] = {q0.x, q0.z, q1.x, q1.z};
-            const unsigned wb[4] = {q0.y, q0.w, q1.y, q1.w};
+        // one node's word from its padded block (slots past its in-links
+        // have an infinite weight) and, when it has more, its later in-links
+        auto node_word = [&](int v, T dv, uint4 q0, uint4 q1) -> unsigned {
+          if (v == src || DT<T>::bits(dv) == DT<T>::kInf) return kPredRoot;
+          const unsigned wx[4] = {q0.x, q0.z, q1.x, q1.z};
+          const unsigned wb[4] = {q0.y, q0.w, q1.y, q1.w};
+          unsigned p = kPredNone;
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-              if (p == kPredNone && j < deg) {
-                const int u = static_cast<int>(wx[j] & 0xffffu);
-                if (!(u < F && u != src)) {
-                  const T du = dS[u];
-                  if (du < dv && DT<T>::add(du, __uint_as_float(wb[j])) == dv) p = wx[j];
-                }
-              }
+          for (int j = 0; j < 4; ++j) {
+            const int u = static_cast<int>(wx[j] & 0xffffu);
+            if (p == kPredNone && !(u < F && u != src)) {
+              const T du = dS[u];
+              if (du < dv && DT<T>::add(du, __uint_as_float(wb[j])) == dv) p = wx[j];
             }
-            for (int i = i0 + 4; p == kPredNone && i < i0 + deg; ++i) {
+          }
+          if (p == kPredNone && ((__ldg(a.r4_more + (v >> 5)) >> (v & 31)) & 1u)) {
+            const int i1 = __ldg(a.g.in_ptr + v + 1);
+            for (int i = __ldg(a.g.in_ptr + v) + 4; p == kPredNone && i < i1; ++i) {
               int u;
               T w;
               rv.load(i, u, w);
@@ -1419,13 +1417,15 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
               if (du < dv && DT<T>::add(du, w) == dv)
                 p = (static_cast<unsigned>(rv.link(i)) << 16) | static_cast<unsigned>(u);
             }
-            if (p == kPredNone) {
-              p = kPredPending;
-              pend = 1;
-            }
           }
-          up[v] = p;
-        }
+          if (p == kPredNone) {
+            pend = 1;
+            return kPredPending;
+          }
+          return p;
+        };
+        for (int v = threadIdx.x; v < n1; v += BLOCK)
+          up[v] = node_word(v, dS[v], __ldg(r4s + 2 * v), __ldg(r4s + 2 * v + 1));
       }
     }
     if (!by_node) {
@@ -2458,6 +2458,13 @@ __global__ void __launch_bounds__(kLinkBlock) k_scen_edits(double* cap, int m, i
   for (int i = ptr[s]; i < ptr[s + 1]; ++i) row[link[i]] = val[i] > 0 ? val[i] : min_pos[s];
 }
 
+// every record of p[n] becomes val
+__global__ void __launch_bounds__(kLinkBlock) k_fill_records(uint2* p, size_t n, uint2 val) {
+  for (size_t i = static_cast<size_t>(blockIdx.x) * kLinkBlock + threadIdx.x; i < n;
+       i += static_cast<size_t>(gridDim.x) * kLinkBlock)
+    p[i] = val;
+}
+
 // rows 1 .. nscen-1 of x [nscen][m] become copies of row 0
 __global__ void __launch_bounds__(kLinkBlock) k_replicate_rows(double* x, int m) {
   const size_t row = static_cast<size_t>(blockIdx.y + 1) * m;
@@ -2509,6 +2516,12 @@ cudaError_t launch_param_rows(unsigned char* rows, const unsigned char* base, in
                               const int* ptr, const int* link, const unsigned char* val, int grid,
                               cudaStream_t s) {
   return launch_param_rows_t(rows, base, m, nscen, ptr, link, val, grid, s);
+}
+
+cudaError_t launch_fill_records(uint2* p, size_t n, uint2 val, int grid, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  k_fill_records<<<grid, kLinkBlock, 0, s>>>(p, n, val);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_replicate_rows(double* x, int m, int nscen, int grid, cudaStream_t s) {

@@ -85,7 +85,9 @@ struct PathArgs {
   const uint2* e4;              // [S][n1][4] the first four records of each node, or nullptr
   const uint2* r32;             // [S][m] {tail, f32 weight bits} in reverse-star order
   const uint2* r4;              // [S][n1][4] the first four in-link records of each node
-                                //     {link << 16 | tail, f32 weight bits}, or nullptr
+                                //     {link << 16 | tail, f32 weight bits} (unused: +inf
+                                //     weight), or nullptr
+  const unsigned* r4_more;      // [ceil(n1/32)] bit v: node v has more than four in-links
   const double* w64;            // [S][m] when fp64 paths
   const int* sources;           // source nodes
   int num_sources;
@@ -210,6 +212,7 @@ cudaError_t launch_param_rows(unsigned char* rows, const unsigned char* base, in
                               cudaStream_t s);
 // rows 1 .. nscen-1 of x [nscen][m] become copies of row 0
 cudaError_t launch_replicate_rows(double* x, int m, int nscen, int grid, cudaStream_t s);
+cudaError_t launch_fill_records(uint2* p, size_t n, uint2 val, int grid, cudaStream_t s);
 int sssp_occupancy(bool fp64, int block, bool smem, int n1, int variant, int m = 0,
                    bool all_global = false);  // CTAs per SM
 int aon_occupancy(bool fp64, int block, bool smem, int n1);

@@ -194,6 +194,7 @@ PathArgs Ctx::path_args(int nscen_slots) const {
              ? e4
              : nullptr;
   a.r4 = rev4 ? r4 : nullptr;
+  a.r4_more = r4_more;
   return a;
 }
 
@@ -279,8 +280,9 @@ int Ctx::ensure_scenarios(int S) {
     TG_TRY(alloc_n(&e4, s4));
     TG_CUDA(cudaMemset(e4, 0, sizeof(uint2) * s4));
     if (rev4) {
+      // slots beyond a node's in-links keep an infinite weight: never tight
       TG_TRY(alloc_n(&r4, s4));
-      TG_CUDA(cudaMemset(r4, 0, sizeof(uint2) * s4));
+      TG_CUDA(launch_fill_records(r4, s4, make_uint2(0u, 0x7f800000u), 2 * num_sms, stream));
     }
   }
   if (opt.record_tape) TG_TRY(alloc_n(&dtdx, sm));
@@ -742,10 +744,16 @@ static int create_impl(const tapgpu_network* net, const tapgpu_demand* dem,
         rpos4[k] = j < 4 ? v * 4 + j : -1;
         rx[k] = (static_cast<unsigned>(k) << 16) | static_cast<unsigned>(c->h_tail[k]);
       }
+      std::vector<unsigned> more((n1 + 31) / 32, 0u);
+      for (int v = 0; v < n1; ++v)
+        if (ip_in[v + 1] - ip_in[v] > 4) more[v >> 5] |= 1u << (v & 31);
       TG_TRY(c->alloc_n(&c->r4_pos, M));
       TG_TRY(c->alloc_n(&c->r4x, M));
+      TG_TRY(c->alloc_n(&c->r4_more, more.size()));
       TG_CUDA(cudaMemcpy(c->r4_pos, rpos4.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
       TG_CUDA(cudaMemcpy(c->r4x, rx.data(), sizeof(unsigned) * M, cudaMemcpyHostToDevice));
+      TG_CUDA(cudaMemcpy(c->r4_more, more.data(), sizeof(unsigned) * more.size(),
+                         cudaMemcpyHostToDevice));
     }
     TG_CUDA(cudaMemcpy(c->e4x, c->h_e4x.data(), sizeof(unsigned) * M, cudaMemcpyHostToDevice));
   }

@@ -54,6 +54,7 @@ struct Ctx {
   bool rev4 = false;
   int* r4_pos = nullptr;    // slot of each link among its head's first four in-links (-1: beyond)
   unsigned* r4x = nullptr;  // first word of each link's padded reverse record (link << 16 | tail)
+  unsigned* r4_more = nullptr;  // bit v: node v has more than four in-links
   double *fft = nullptr, *alpha = nullptr, *beta = nullptr;
   unsigned char* ipow = nullptr;
 
