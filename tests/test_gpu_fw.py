@@ -46,6 +46,69 @@ def test_aon_matches_oracle(built_lib, grid416):
             assert _rel(y, ref) < 1e-12
 
 
+def _hub_network():
+    """grid416 plus six extra in-links into each of twenty hub nodes (in-degree
+    up to ten), from random tails with free-flow times that make some of them
+    the shortest way in: predecessors then also come from beyond a node's
+    first four in-links (the loading kernel's padded block)."""
+    net, dem = synth.make_grid416()
+    rng = np.random.default_rng(20261204)
+    n = net.num_nodes
+    have = set(zip(net.init.tolist(), net.term.tolist()))
+    hubs = rng.choice(np.arange(net.first_thru_node, n + 1), 20, replace=False)
+    mean_fft = float(np.mean(net.fft))
+    u, v = [], []
+    for h in hubs:
+        added = 0
+        while added < 6:
+            t = int(rng.integers(1, n + 1))
+            if t == h or (t, int(h)) in have:
+                continue
+            have.add((t, int(h)))
+            u.append(t)
+            v.append(int(h))
+            added += 1
+    k = len(u)
+    # shortcuts of a few grid hops' free-flow time: some win, some do not
+    fft = mean_fft * rng.uniform(1.0, 8.0, k)
+    ext = synth.Network(
+        num_nodes=n, num_zones=net.num_zones, first_thru_node=net.first_thru_node,
+        init=np.concatenate([net.init, np.asarray(u, np.int64)]),
+        term=np.concatenate([net.term, np.asarray(v, np.int64)]),
+        capacity=np.concatenate([net.capacity, np.full(k, float(np.median(net.capacity)))]),
+        length=np.concatenate([net.length, np.ones(k)]),
+        fft=np.concatenate([net.fft, fft]),
+        alpha=np.concatenate([net.alpha, np.full(k, 0.15)]),
+        beta=np.concatenate([net.beta, np.full(k, 4.0)]),
+        speed=np.concatenate([net.speed, np.zeros(k)]),
+        toll=np.concatenate([net.toll, np.zeros(k)]),
+        link_type=np.concatenate([net.link_type, np.full(k, 9, np.int16)]),  # (extra links)
+        x=net.x, y=net.y).sort_links()
+    return ext, dem
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_high_in_degree_nodes(built_lib, precision):
+    """Nodes with up to ten in-links: the predecessor of such a node may be its
+    fifth or later in-link, which the per-node scan reads past the node's
+    padded block; flows, costs, relative gap and VHT against the oracle."""
+    net, dem = _hub_network()
+    deg = np.bincount(net.term, minlength=net.num_nodes + 1)
+    assert deg.max() >= 8 and int((deg > 4).sum()) >= 20
+    iters = 25
+    ref = oracle.frankwolfe(net, dem, threads=1, max_iters=iters)
+    with Solver(net, dem, precision=precision) as s:
+        r = s.solve(max_iters=iters)
+        x, t = s.flows()
+    assert r["iterations"] == iters and r["error_bits"] == 0
+    tol = RTOL64 if precision == "fp64" else RTOL32
+    assert _rel(x, ref["x"]) < tol
+    assert abs(r["total_cost"] - ref["total_cost"]) <= tol * abs(ref["total_cost"])
+    assert abs(r["relgap"] - ref["relgap"]) <= tol * abs(ref["relgap"])
+    # some hubs are entered through the extra links
+    assert float(x[net.link_type == 9].sum()) > 0
+
+
 VARIANTS = ["rounds", "async", "nearfar", "nearfar_queue", "small"]
 
 
