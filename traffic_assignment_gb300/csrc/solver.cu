@@ -357,6 +357,13 @@ int Ctx::plan_launches() {
   const size_t room = optin > 1024 ? static_cast<size_t>(optin - 1024) : 0;
   sssp_smem = sssp_smem_bytes(n1, fp64, sssp_variant, M) <= room && !opt.global_scratch;
   aon_smem = aon_smem_bytes(n1, fp64) <= room && !opt.global_scratch;
+  // near-far kernels whose shared memory leaves at most four 256-thread CTAs
+  // per SM (FP64 labels of a 10k-node network: two) take 512 threads, so
+  // that each task has more warps in flight (10k nodes, FP64: 77.0 -> 67.5 ms
+  // per 64-scenario iteration)
+  if (opt.sssp_block <= 0 && nf && sssp_smem &&
+      sssp_occupancy(fp64, 256, true, n1, sssp_variant, M) * 256 <= 1024)
+    sssp_block = 512;
   int so = sssp_occupancy(fp64, sssp_block, sssp_smem, n1, sssp_variant, M, opt.global_scratch == 2);
   int ao = aon_occupancy(fp64, aon_block, aon_smem, n1);
   if (so <= 0 || ao <= 0) {
