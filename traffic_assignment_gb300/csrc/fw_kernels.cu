@@ -1317,16 +1317,19 @@ __device__ __forceinline__ int parent_of(const int* parent, const unsigned short
   }
 }
 
-// COMPACT (FP32 labels, at most 65535 nodes): 8 bytes per node hold the
-// labels and the predecessor words, the labels' half later the 32-bit node
-// totals; parents are 16-bit (the task's slot of the label buffer serves as
-// scratch once its labels are in shared memory).  10 bytes per node let
-// two CTAs share an SM up to ~11,500 nodes, so that one task's longest walks
-// overlap another task's work.  Otherwise 16 bytes per node: totals (labels
-// first), predecessor links, parents.
+// COMPACT (at most 65535 nodes): 10 bytes per node, so that two CTAs share
+// an SM up to ~11,500 nodes and one task's longest walks overlap another
+// task's work.  FP32 labels: 8 bytes per node hold the labels and the
+// predecessor words, the labels' half later the 32-bit node totals; FP64
+// labels (with the padded in-link records): 8 bytes per node hold the labels,
+// later the 64-bit totals, and the predecessor words go to the task's slot of
+// the label buffer, free once its labels are in shared memory (its second
+// half serves as scratch); parents are 16-bit.  Otherwise 16 bytes per node:
+// totals (labels first), predecessor links, parents.
 template <typename T, int BLOCK, bool SMEM, bool COMPACT>
-__global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathArgs a) {
-  static_assert(!COMPACT || sizeof(T) == 4, "the compact layout holds 4-byte labels");
+__global__ void __launch_bounds__(BLOCK, COMPACT ? (sizeof(T) == 4 ? 2048 : 1024) / BLOCK : 1)
+    k_aon(PathArgs a) {
+  constexpr bool kPredGlobal = COMPACT && sizeof(T) == 8;  // predecessor words in the label slot
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int sh_task;
   __shared__ unsigned long long sh_red[BLOCK / 32];
@@ -1357,8 +1360,10 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
     const RevEdges<T> rv = rev_edges_of<T>(a, scen);
     const T* din = static_cast<const T*>(a.dist) + static_cast<size_t>(task - a.task_begin) * n1;
     // COMPACT: the slot's labels are copied below; it then serves as scratch
+    // (FP64: its first half holds the predecessor words)
     int* gslot = reinterpret_cast<int*>(const_cast<T*>(din));
-    int* scr = COMPACT ? gslot : parent;
+    int* scr = COMPACT ? (kPredGlobal ? gslot + n1 : gslot) : parent;
+    int* predw = kPredGlobal ? gslot : pred;
 
     // labels in, several loads in flight per thread; predecessors cleared
     {
@@ -1376,10 +1381,10 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
     // nodes both fit 16 bits (the compact layout), so that the parents need
     // no lookup of the link's tail; the minimum still orders by link.
     const bool pack = COMPACT && a.g.m <= 0xffff;
-    unsigned* up = reinterpret_cast<unsigned*>(pred);
+    unsigned* up = reinterpret_cast<unsigned*>(predw);
     int pend = 0;
     bool by_node = false;
-    if constexpr (COMPACT) {
+    if constexpr (COMPACT && sizeof(T) == 4) {
       if (pack && a.r4) {
         // The same predecessors, node by node: each node's first four
         // in-links come from one padded 32-byte block of {link << 16 | tail,
@@ -1428,7 +1433,56 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
           up[v] = node_word(v, dS[v], __ldg(r4s + 2 * v), __ldg(r4s + 2 * v + 1));
       }
     }
+    if constexpr (kPredGlobal) {
+      if (a.r4d) {
+        // FP64 labels, node by node as above: a node's first four in-links
+        // are one padded 64-byte block of {link, tail, weight} records; each
+        // node's word goes once, without atomics, to the label slot
+        by_node = true;
+        __syncthreads();  // (labels in: the slot is free from here)
+        const uint4* r4s = a.r4d + static_cast<size_t>(scen) * n1 * 4;
+        for (int v = threadIdx.x; v < n1; v += BLOCK) {
+          const T dv = dS[v];
+          unsigned p = kPredRoot;
+          if (v != src && DT<T>::bits(dv) != DT<T>::kInf) {
+            p = kPredNone;
+            uint4 r[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) r[j] = __ldg(r4s + 4 * static_cast<size_t>(v) + j);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              const int u = static_cast<int>(r[j].y);
+              if (p == kPredNone && !(u < F && u != src)) {
+                const T du = dS[u];
+                const T w = __hiloint2double(static_cast<int>(r[j].w), static_cast<int>(r[j].z));
+                if (du < dv && DT<T>::add(du, w) == dv) p = pack ? (r[j].x << 16) | r[j].y : r[j].x;
+              }
+            }
+            if (p == kPredNone && ((__ldg(a.r4_more + (v >> 5)) >> (v & 31)) & 1u)) {
+              const int i1 = __ldg(a.g.in_ptr + v + 1);
+              for (int i = __ldg(a.g.in_ptr + v) + 4; p == kPredNone && i < i1; ++i) {
+                int u;
+                T w;
+                rv.load(i, u, w);
+                if (u < F && u != src) continue;
+                const T du = dS[u];
+                if (du < dv && DT<T>::add(du, w) == dv) {
+                  const unsigned k = static_cast<unsigned>(rv.link(i));
+                  p = pack ? (k << 16) | static_cast<unsigned>(u) : k;
+                }
+              }
+            }
+            if (p == kPredNone) {
+              p = kPredPending;
+              pend = 1;
+            }
+          }
+          up[v] = p;
+        }
+      }
+    }
     if (!by_node) {
+      if constexpr (kPredGlobal) __syncthreads();  // (the words overwrite the slot's labels)
       for (int v = threadIdx.x; v < n1; v += BLOCK) up[v] = kPredNone;
       __syncthreads();
 
@@ -1659,7 +1713,7 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
             k[j] = COMPACT && pack ? up[v] >> 16 : up[v];
           } else {
             q[j] = static_cast<unsigned long long>(thr[v]);
-            k[j] = static_cast<unsigned>(pred[v]);
+            k[j] = COMPACT && pack ? up[v] >> 16 : up[v];
           }
         }
 #pragma unroll
@@ -1679,7 +1733,11 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? 2048 / BLOCK : 1) k_aon(PathA
         }
       } else {
         const long long q = thr[v];
-        if (q != 0) atomicAdd(y + pred[v], static_cast<unsigned long long>(q));
+        if (q != 0) {
+          const unsigned pw = up[v];
+          const unsigned k = COMPACT && pack ? pw >> 16 : pw;
+          atomicAdd(y + k, static_cast<unsigned long long>(q));
+        }
       }
     }
   }
@@ -1777,7 +1835,17 @@ __device__ __forceinline__ void write_weights(const LinkArgs& a, int scen, int k
       if (p >= 0) a.r4[static_cast<size_t>(scen) * a.n1 * 4 + p] = make_uint2(__ldg(a.r4x + k), bits);
     }
   }
-  if (a.w64) a.w64[i] = t;
+  if (a.w64) {
+    a.w64[i] = t;
+    if (a.r4d) {
+      const int p = __ldg(a.r4_pos + k);
+      if (p >= 0)
+        a.r4d[static_cast<size_t>(scen) * a.n1 * 4 + p] =
+            make_uint4(static_cast<unsigned>(k), static_cast<unsigned>(__ldg(a.tail + k)),
+                       static_cast<unsigned>(__double2loint(t)),
+                       static_cast<unsigned>(__double2hiint(t)));
+    }
+  }
 }
 
 constexpr int kLinkBlock = 256;
@@ -2283,9 +2351,9 @@ bool nfq_split(int n1, int variant) {
 // scratch, so they are rounded to 16 bytes (8-byte totals and labels).
 bool aon_compact(int n1, bool fp64) { return !fp64 && n1 <= 0xffff; }
 
-size_t aon_smem_bytes(int n1, bool fp64) {
+size_t aon_smem_bytes(int n1, bool fp64, bool c64) {
   const size_t n = static_cast<size_t>(n1);
-  if (aon_compact(n1, fp64)) return align16(align16(8 * n) + align16(2 * n));
+  if (aon_compact(n1, fp64) || (fp64 && c64)) return align16(align16(8 * n) + align16(2 * n));
   return align16(align16(8 * n) + 2 * 4 * n);
 }
 
@@ -2318,10 +2386,13 @@ cudaError_t launch_sssp(const PathArgs& a, bool fp64, int grid, int block, bool 
 
 cudaError_t launch_aon(const PathArgs& a, bool fp64, int grid, int block, bool smem,
                        cudaStream_t s) {
-  const size_t bytes = aon_smem_bytes(a.g.n1, fp64);
+  const bool c64 = fp64 && a.aon_c64;
+  const size_t bytes = aon_smem_bytes(a.g.n1, fp64, c64);
   const bool compact = aon_compact(a.g.n1, fp64);
 #define TAPGPU_AON_CASE(B)                                                               \
   if (block == B) {                                                                      \
+    if (c64) return smem ? launch_aon_t<double, B, true, true>(a, grid, bytes, s)        \
+                         : launch_aon_t<double, B, false, true>(a, grid, bytes, s);      \
     if (fp64) return smem ? launch_aon_t<double, B, true, false>(a, grid, bytes, s)      \
                           : launch_aon_t<double, B, false, false>(a, grid, bytes, s);    \
     if (compact) return smem ? launch_aon_t<float, B, true, true>(a, grid, bytes, s)     \
@@ -2381,11 +2452,13 @@ int sssp_occupancy(bool fp64, int block, bool smem, int n1, int variant, int m, 
   return 0;
 }
 
-int aon_occupancy(bool fp64, int block, bool smem, int n1) {
-  const size_t bytes = aon_smem_bytes(n1, fp64);
+int aon_occupancy(bool fp64, int block, bool smem, int n1, bool c64) {
+  const size_t bytes = aon_smem_bytes(n1, fp64, c64);
   const bool compact = aon_compact(n1, fp64);
 #define TAPGPU_OCC(B)                                                                     \
   if (block == B) {                                                                       \
+    if (fp64 && c64) return smem ? occ_aon_t<double, B, true, true>(bytes)                \
+                                 : occ_aon_t<double, B, false, true>(bytes);              \
     if (fp64) return smem ? occ_aon_t<double, B, true, false>(bytes)                      \
                           : occ_aon_t<double, B, false, false>(bytes);                    \
     if (compact) return smem ? occ_aon_t<float, B, true, true>(bytes)                     \
@@ -2465,6 +2538,12 @@ __global__ void __launch_bounds__(kLinkBlock) k_fill_records(uint2* p, size_t n,
     p[i] = val;
 }
 
+__global__ void __launch_bounds__(kLinkBlock) k_fill_records4(uint4* p, size_t n, uint4 val) {
+  for (size_t i = static_cast<size_t>(blockIdx.x) * kLinkBlock + threadIdx.x; i < n;
+       i += static_cast<size_t>(gridDim.x) * kLinkBlock)
+    p[i] = val;
+}
+
 // rows 1 .. nscen-1 of x [nscen][m] become copies of row 0
 __global__ void __launch_bounds__(kLinkBlock) k_replicate_rows(double* x, int m) {
   const size_t row = static_cast<size_t>(blockIdx.y + 1) * m;
@@ -2521,6 +2600,12 @@ cudaError_t launch_param_rows(unsigned char* rows, const unsigned char* base, in
 cudaError_t launch_fill_records(uint2* p, size_t n, uint2 val, int grid, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   k_fill_records<<<grid, kLinkBlock, 0, s>>>(p, n, val);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill_records4(uint4* p, size_t n, uint4 val, int grid, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  k_fill_records4<<<grid, kLinkBlock, 0, s>>>(p, n, val);
   return cudaGetLastError();
 }
 

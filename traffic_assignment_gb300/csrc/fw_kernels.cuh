@@ -88,6 +88,9 @@ struct PathArgs {
                                 //     {link << 16 | tail, f32 weight bits} (unused: +inf
                                 //     weight), or nullptr
   const unsigned* r4_more;      // [ceil(n1/32)] bit v: node v has more than four in-links
+  const uint4* r4d;             // [S][n1][4] FP64 paths: the first four in-link records of each
+                                //     node {link, tail, f64 weight} (unused: +inf), or nullptr
+  int aon_c64;                  // FP64 loading in the compact layout (with r4d)
   const double* w64;            // [S][m] when fp64 paths
   const int* sources;           // source nodes
   int num_sources;
@@ -130,6 +133,7 @@ struct LinkArgs {
   int n1;
   uint2* r32;                   // [S][m] packed fp32 reverse records (with e32)
   uint2* r4;                    // [S][n1][4] first four in-link records of each node, or nullptr
+  uint4* r4d;                   // [S][n1][4] the same for FP64 paths {link, tail, weight}, or nullptr
   const int* r4_pos;            // [m] slot of link k among its head's four (-1: beyond the fourth)
   const unsigned* r4x;          // [m] first word of link k's padded reverse record
   const int* head;              // [m] head node of each link (for e32)
@@ -165,7 +169,8 @@ size_t sssp_smem_bytes(int n1, bool fp64, int variant = 0, int m = 0);
 // and ring in shared memory (these bytes) while they fit.
 size_t nfq_split_smem_bytes(int n1, int variant);
 bool nfq_split(int n1, int variant);
-size_t aon_smem_bytes(int n1, bool fp64);
+// c64: FP64 labels in the compact layout (predecessor words in the label slot)
+size_t aon_smem_bytes(int n1, bool fp64, bool c64 = false);
 bool aon_compact(int n1, bool fp64);  // 10-byte-per-node loading layout
 int max_smem_optin(int device);
 // shortest-path kernel variants
@@ -213,8 +218,9 @@ cudaError_t launch_param_rows(unsigned char* rows, const unsigned char* base, in
 // rows 1 .. nscen-1 of x [nscen][m] become copies of row 0
 cudaError_t launch_replicate_rows(double* x, int m, int nscen, int grid, cudaStream_t s);
 cudaError_t launch_fill_records(uint2* p, size_t n, uint2 val, int grid, cudaStream_t s);
+cudaError_t launch_fill_records4(uint4* p, size_t n, uint4 val, int grid, cudaStream_t s);
 int sssp_occupancy(bool fp64, int block, bool smem, int n1, int variant, int m = 0,
                    bool all_global = false);  // CTAs per SM
-int aon_occupancy(bool fp64, int block, bool smem, int n1);
+int aon_occupancy(bool fp64, int block, bool smem, int n1, bool c64 = false);
 
 }  // namespace tapgpu

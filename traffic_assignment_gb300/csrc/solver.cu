@@ -194,6 +194,8 @@ PathArgs Ctx::path_args(int nscen_slots) const {
              ? e4
              : nullptr;
   a.r4 = rev4 ? r4 : nullptr;
+  a.r4d = fp64 ? r4d : nullptr;
+  a.aon_c64 = aon_c64 ? 1 : 0;
   a.r4_more = r4_more;
   return a;
 }
@@ -216,6 +218,7 @@ LinkArgs Ctx::link_args(int nscen) const {
   a.ell_pos = ell_pos;
   a.e4x = e4x;
   a.r4 = rev4 && !fp64 ? r4 : nullptr;
+  a.r4d = fp64 ? r4d : nullptr;
   a.r4_pos = r4_pos;
   a.r4x = r4x;
   a.n1 = n1;
@@ -248,14 +251,15 @@ LinkArgs Ctx::link_args(int nscen) const {
 int Ctx::ensure_scenarios(int S) {
   if (S <= S_cap) return TAPGPU_OK;
   // release the old per-scenario arrays
-  void* olds[] = {cap, x, t, d, dtdx, yfx, e32, r32, e4, r4, w64, state, partials, arrive, trace,
-                  scen_list, x_hist, d_hist, lam_hist};
+  void* olds[] = {cap, x, t, d, dtdx, yfx, e32, r32, e4, r4, r4d, w64, state, partials, arrive,
+                  trace, scen_list, x_hist, d_hist, lam_hist};
   for (void* p : olds) free_owned(this, p);
   cap = x = t = d = dtdx = nullptr;
   yfx = nullptr;
   e32 = nullptr;
   e4 = nullptr;
   r4 = nullptr;
+  r4d = nullptr;
   r32 = nullptr;
   w64 = nullptr;
   state = nullptr;
@@ -270,9 +274,13 @@ int Ctx::ensure_scenarios(int S) {
   TG_TRY(alloc_n(&t, sm));
   TG_TRY(alloc_n(&d, sm));
   TG_TRY(alloc_n(&yfx, sm));
-  if (fp64)
+  if (fp64) {
     TG_TRY(alloc_n(&w64, sm));
-  else
+    // slots beyond a node's in-links keep an infinite weight: never tight
+    const size_t s4 = static_cast<size_t>(S) * n1 * 4;
+    TG_TRY(alloc_n(&r4d, s4));
+    TG_CUDA(launch_fill_records4(r4d, s4, make_uint4(0u, 0u, 0u, 0x7ff00000u), 2 * num_sms, stream));
+  } else
   {
     TG_TRY(alloc_n(&e32, sm));
     TG_TRY(alloc_n(&r32, sm));
@@ -352,11 +360,14 @@ int Ctx::plan_launches() {
   if ((sssp_variant == kSsspNearFarQueue || sssp_variant == kSsspNearFarQueueWide) &&
       sssp_block >= kQueueSlots)
     sssp_block = 256;
-  aon_block = opt.aon_block > 0 ? opt.aon_block : 1024;
+  // FP64 loading in the compact layout (10 bytes per node, two 512-thread
+  // CTAs per SM) up to 65535 nodes
+  aon_c64 = fp64 && n1 <= 0xffff && !opt.global_scratch;
+  aon_block = opt.aon_block > 0 ? opt.aon_block : (aon_c64 ? 512 : 1024);
   // leave room for the kernels' static shared memory (a few words)
   const size_t room = optin > 1024 ? static_cast<size_t>(optin - 1024) : 0;
   sssp_smem = sssp_smem_bytes(n1, fp64, sssp_variant, M) <= room && !opt.global_scratch;
-  aon_smem = aon_smem_bytes(n1, fp64) <= room && !opt.global_scratch;
+  aon_smem = aon_smem_bytes(n1, fp64, aon_c64) <= room && !opt.global_scratch;
   // near-far kernels whose shared memory leaves at most four 256-thread CTAs
   // per SM (FP64 labels of a 10k-node network: two) take 512 threads, so
   // that each task has more warps in flight (10k nodes, FP64: 77.0 -> 67.5 ms
@@ -365,7 +376,7 @@ int Ctx::plan_launches() {
       sssp_occupancy(fp64, 256, true, n1, sssp_variant, M) * 256 <= 1024)
     sssp_block = 512;
   int so = sssp_occupancy(fp64, sssp_block, sssp_smem, n1, sssp_variant, M, opt.global_scratch == 2);
-  int ao = aon_occupancy(fp64, aon_block, aon_smem, n1);
+  int ao = aon_occupancy(fp64, aon_block, aon_smem, n1, aon_c64);
   if (so <= 0 || ao <= 0) {
     set_message("no resident CTA fits for the shortest-path kernels");
     return TAPGPU_ERR_UNSUPPORTED;
@@ -376,7 +387,7 @@ int Ctx::plan_launches() {
   aon_grid = ao * num_sms;
   size_t scratch = 0;
   if (!sssp_smem) scratch = std::max(scratch, sssp_smem_bytes(n1, fp64, sssp_variant, M) * sssp_grid);
-  if (!aon_smem) scratch = std::max(scratch, aon_smem_bytes(n1, fp64) * aon_grid);
+  if (!aon_smem) scratch = std::max(scratch, aon_smem_bytes(n1, fp64, aon_c64) * aon_grid);
   if (scratch) {
     TG_TRY(alloc(&path_scratch, scratch));
     path_scratch_bytes = scratch;
@@ -399,6 +410,7 @@ int Ctx::enqueue_paths(int nscen, bool load, const uint2* e32p, const uint2* r32
     a.e32 = e32p;
     a.r32 = r32p;
     if (r32p != r32) a.r4 = nullptr;  // (the padded reverse records follow the context's own)
+    if (w64p != w64) a.r4d = nullptr;
     a.w64 = w64p;
     a.y_fx = ydst;
     a.do_load = load ? 1 : 0;
@@ -419,7 +431,7 @@ int Ctx::enqueue_paths(int nscen, bool load, const uint2* e32p, const uint2* r32
                         stream));
     if (measuring) TG_TRY(mark(0, false));
     a.counter = counters + 1;
-    a.scratch_stride = static_cast<long long>(aon_smem_bytes(n1, fp64));
+    a.scratch_stride = static_cast<long long>(aon_smem_bytes(n1, fp64, aon_c64));
     if (measuring) TG_TRY(mark(1, true));
     TG_CUDA(launch_aon(a, fp64, std::min(aon_grid, ntask), aon_block, aon_smem, stream));
     if (measuring) TG_TRY(mark(1, false));
@@ -742,25 +754,30 @@ static int create_impl(const tapgpu_network* net, const tapgpu_demand* dem,
     }
     TG_CUDA(cudaMemcpy(c->out_deg, deg.data(), sizeof(int) * n1, cudaMemcpyHostToDevice));
     TG_CUDA(cudaMemcpy(c->ell_pos, pos.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
+    // padded reverse records: FP64 paths always ({link, tail, weight}),
+    // FP32 paths when nodes and links fit 16 bits ({link << 16 | tail, weight})
     c->rev4 = !c->fp64 && n1 <= 0xffff && M <= 0xffff;
-    if (c->rev4) {
+    if (c->rev4 || c->fp64) {
       std::vector<int> rpos4(M);
-      std::vector<unsigned> rx(M);
       for (int k = 0; k < M; ++k) {
         const int v = c->h_head[k], j = c->h_rpos[k] - ip_in[v];
         rpos4[k] = j < 4 ? v * 4 + j : -1;
-        rx[k] = (static_cast<unsigned>(k) << 16) | static_cast<unsigned>(c->h_tail[k]);
       }
       std::vector<unsigned> more((n1 + 31) / 32, 0u);
       for (int v = 0; v < n1; ++v)
         if (ip_in[v + 1] - ip_in[v] > 4) more[v >> 5] |= 1u << (v & 31);
       TG_TRY(c->alloc_n(&c->r4_pos, M));
-      TG_TRY(c->alloc_n(&c->r4x, M));
       TG_TRY(c->alloc_n(&c->r4_more, more.size()));
       TG_CUDA(cudaMemcpy(c->r4_pos, rpos4.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
-      TG_CUDA(cudaMemcpy(c->r4x, rx.data(), sizeof(unsigned) * M, cudaMemcpyHostToDevice));
       TG_CUDA(cudaMemcpy(c->r4_more, more.data(), sizeof(unsigned) * more.size(),
                          cudaMemcpyHostToDevice));
+    }
+    if (c->rev4) {
+      std::vector<unsigned> rx(M);
+      for (int k = 0; k < M; ++k)
+        rx[k] = (static_cast<unsigned>(k) << 16) | static_cast<unsigned>(c->h_tail[k]);
+      TG_TRY(c->alloc_n(&c->r4x, M));
+      TG_CUDA(cudaMemcpy(c->r4x, rx.data(), sizeof(unsigned) * M, cudaMemcpyHostToDevice));
     }
     TG_CUDA(cudaMemcpy(c->e4x, c->h_e4x.data(), sizeof(unsigned) * M, cudaMemcpyHostToDevice));
   }
@@ -1527,6 +1544,8 @@ int tapgpu_sssp(tapgpu_ctx* ctx, const double* weights, const int64_t* srcs, int
     a.w64 = c->api_w64;
     a.e32 = nullptr;
     a.r4 = nullptr;
+    a.r4d = nullptr;
+    a.aon_c64 = 0;
     a.do_load = 0;
     a.pred_out = c->pred_buf;
     a.y_fx = c->api_yfx;
@@ -1738,7 +1757,7 @@ int tapgpu_profile_iteration(tapgpu_ctx* ctx, int reps, float* ms) {
                         c->sssp_smem, c->sssp_variant, c->stream);
     cudaEventRecord(ev[1], c->stream);
     a.counter = c->counters + 1;
-    a.scratch_stride = static_cast<long long>(tapgpu::aon_smem_bytes(c->n1, c->fp64));
+    a.scratch_stride = static_cast<long long>(tapgpu::aon_smem_bytes(c->n1, c->fp64, c->aon_c64));
     tapgpu::launch_aon(a, c->fp64, std::min<int64_t>(c->aon_grid, tasks), c->aon_block,
                        c->aon_smem, c->stream);
     cudaEventRecord(ev[2], c->stream);

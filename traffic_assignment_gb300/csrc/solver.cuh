@@ -91,6 +91,8 @@ struct Ctx {
   uint2* r32 = nullptr;  // packed {tail, f32 weight} per scenario, reverse-star order
   uint2* e4 = nullptr;   // per scenario, the first four records of each node (padded)
   uint2* r4 = nullptr;   // per scenario, the first four in-link records of each node (padded)
+  uint4* r4d = nullptr;  // the same for FP64 paths: {link, tail, f64 weight}
+  bool aon_c64 = false;  // FP64 loading in the compact layout (predecessor words in the label slot)
   int* rpos = nullptr;   // reverse-star slot of each link
   std::vector<int> h_rpos;
   double* w64 = nullptr;
