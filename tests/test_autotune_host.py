@@ -9,8 +9,9 @@ from traffic_assignment_gb300 import synth
 def test_candidates_cover_every_variant_and_block():
     c = A.candidates()
     assert {x.sssp_variant for x in c} == {"rounds", "async", "nearfar", "nearfar_queue"}
-    assert {x.sssp_block for x in c} == {128, 256, 512, 1024}
-    assert {x.aon_block for x in c} == {256, 512, 1024}
+    # (0: the library's choice for the precision and network size)
+    assert {x.sssp_block for x in c} == {0, 128, 256, 512, 1024}
+    assert {x.aon_block for x in c} == {0, 256, 512, 1024}
     assert len(set(c)) == len(c)
     q = A.candidates(quick=True)
     assert set(q) <= set(c)

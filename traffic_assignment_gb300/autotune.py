@@ -43,7 +43,7 @@ class Candidate:
     sssp_variant: str = "nearfar_queue"
     sssp_block: int = 256
     nf_scale: float = 16.0  # near-far step = nf_scale x mean free-flow time
-    aon_block: int = 1024
+    aon_block: int = 0  # 0: the library's choice for the precision and network size
 
     def solver_kwargs(self, net: Network) -> Dict:
         kw = dict(sssp_variant=self.sssp_variant, sssp_block=self.sssp_block,
@@ -71,8 +71,10 @@ SMALL_NET = 4096
 
 
 def candidates(quick: bool = False, net: Optional[Network] = None) -> List[Candidate]:
-    """The sweep: every variant x block, and near-far x step scale; with a
-    small network (at most SMALL_NET nodes and links) the edge-list sweeps too."""
+    """The sweep: every variant x block, and near-far x step scale, with the
+    library's loading shape; then the loading kernel's block at the library's
+    shortest-path shape (block 0: the library's choice); with a small network
+    (at most SMALL_NET nodes and links) the edge-list sweeps too."""
     out = []
     blocks = (256, 512) if quick else (128, 256, 512, 1024)
     scales = (8.0, 16.0, 32.0) if quick else (4.0, 8.0, 16.0, 32.0, 64.0)
@@ -82,11 +84,11 @@ def candidates(quick: bool = False, net: Optional[Network] = None) -> List[Candi
     for v in variants:
         for b in blocks:
             if v.startswith("nearfar"):
-                out.extend(Candidate(v, b, s, 1024) for s in scales)
+                out.extend(Candidate(v, b, s, 0) for s in scales)
             else:
-                out.append(Candidate(v, b, 16.0, 1024))
+                out.append(Candidate(v, b, 16.0, 0))
     # the loading kernel's block, at the default shortest-path shape
-    out.extend(Candidate("nearfar_queue", 256, 16.0, a) for a in (256, 512))
+    out.extend(Candidate("nearfar_queue", 0, 16.0, a) for a in (256, 512, 1024))
     return out
 
 
