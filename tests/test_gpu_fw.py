@@ -109,6 +109,44 @@ def test_high_in_degree_nodes(built_lib, precision):
     assert float(x[net.link_type == 9].sum()) > 0
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_compact_layout_with_wide_link_ids(built_lib, precision):
+    """22,500 nodes but ~90,000 links: the compact loading layouts whose
+    predecessor words are plain link ids (parents looked up by link), FP32
+    with the slot sweep into shared memory, FP64 with the per-node scan into
+    the label slot; against the oracle (FP32 paths: the bounds of the
+    100k-node test)."""
+    net, dem = synth.make_grid22k()
+    assert net.num_nodes + 1 <= 0xffff < net.num_links
+    iters = 8
+    ref = oracle.frankwolfe(net, dem, threads=os.cpu_count() or 1, max_iters=iters)
+    with Solver(net, dem, precision=precision) as s:
+        r = s.solve(max_iters=iters)
+        x, _ = s.flows()
+    assert r["error_bits"] == 0 and r["iterations"] == iters
+    if precision == "fp64":
+        assert _rel(x, ref["x"]) < RTOL64
+        assert abs(r["total_cost"] - ref["total_cost"]) <= RTOL64 * ref["total_cost"]
+        assert abs(r["relgap"] - ref["relgap"]) <= RTOL64 * abs(ref["relgap"])
+    else:
+        assert abs(r["total_cost"] - ref["total_cost"]) <= RTOL32 * ref["total_cost"]
+        assert np.abs(x - ref["x"]).sum() <= 1e-3 * np.abs(ref["x"]).sum()
+
+
+def test_resident_cta_caps_keep_results(built_lib):
+    """Capping the resident CTAs per SM of both path kernels changes only the
+    schedule: the least fixed point of the relaxations, the trees and the
+    integer loads are the same, bit for bit."""
+    net, dem = synth.make_grid3600()
+    outs = []
+    for kw in ({}, dict(sssp_ctas_per_sm=1, aon_ctas_per_sm=1), dict(sssp_ctas_per_sm=3)):
+        with Solver(net, dem, precision="fp32", **kw) as s:
+            s.solve(max_iters=10)
+            outs.append(s.flows()[0])
+    np.testing.assert_array_equal(outs[1], outs[0])
+    np.testing.assert_array_equal(outs[2], outs[0])
+
+
 VARIANTS = ["rounds", "async", "nearfar", "nearfar_queue", "small"]
 
 

@@ -394,6 +394,13 @@ def make_grid3600(seed: int = 1007):
     return _arterial_grid(seed, 60, 40, 100, 1.5e5, 15.0)
 
 
+def make_grid22k(seed: int = 1008):
+    """150 x 150 grid + 300 arterials, 150 zones: 22,500 nodes (16-bit node
+    ids) but ~90,000 links (beyond 16 bits), a test network for the compact
+    loading layouts with plain link ids as predecessor words."""
+    return _arterial_grid(seed, 150, 300, 150, 3.0e5, 30.0)
+
+
 def make_grid100k(seed: int = 1005, num_zones: int = 4000):
     """316 x 316 grid + arterials: 99,856 nodes, ~400,000 links, 4,000 zones."""
     return _arterial_grid(seed, 316, 2000, num_zones, 15.0e6, 60.0)
@@ -436,6 +443,7 @@ def make_workload(name: str, seed: Optional[int] = None):
         "small24": make_small24,
         "grid416": make_grid416,
         "grid3600": make_grid3600,
+        "grid22k": make_grid22k,
         "grid10k": make_grid10k,
         "grid100k": make_grid100k,
     }
