@@ -2113,38 +2113,11 @@ __device__ void ls_fallback_block(const LinkArgs& a, int scen, ScenState& st, do
   }
 }
 
-// The line search after the passes already launched (a.pass of them), by
-// one block per scenario: the remaining passes' candidate batches (the
-// arithmetic of k_ls_pass, block-wide sums), then the one-at-a-time fallback.
-// Small networks launch only the first pass before it: that pass tries
-// 2^-1 .. 2^-12, so this launch usually returns at once, one launch instead
-// of one per pass.
-constexpr int kLsRestBlock = 512;
-__global__ void __launch_bounds__(kLsRestBlock) k_ls_fallback(LinkArgs a) {
-  __shared__ double sh[kNumSums * (kLsRestBlock / 32)];
+__global__ void __launch_bounds__(1024) k_ls_fallback(LinkArgs a) {
+  __shared__ double sh[32];
   __shared__ int sh_found;
   const int scen = scen_of(a);
-  ScenState& st = a.state[scen];
-  if (st.done || !st.ls_pending) return;  // (read by every thread before any change to it)
-  const size_t off = static_cast<size_t>(scen) * a.m;
-  const double* cap = a.cap + off;
-  const int passes = a.ls_mode == kLsExact ? kLsExactPasses : kLsPasses;
-  for (int pass = a.pass; pass < passes; ++pass) {
-    if (!st.ls_pending) break;  // (uniform: written before the last barrier)
-    const int e0 = st.ls_next;
-    const double blo = st.ls_lo, bhi = st.ls_hi;
-    double acc[kNumSums];
-#pragma unroll
-    for (int i = 0; i < kNumSums; ++i) acc[i] = 0.0;
-    for (int k = threadIdx.x; k < a.m; k += kLsRestBlock)
-      ls_link(a, scen, off, cap, k, pass, e0, blo, bhi, acc);
-    block_sum<kNumSums, kLsRestBlock>(acc, sh);
-    if (threadIdx.x == 0)
-      ls_decide(st, acc, e0, pass, a.total_demand_s ? a.total_demand_s[scen] : a.total_demand,
-                a.ls_mode);
-    __syncthreads();
-  }
-  ls_fallback_block(a, scen, st, sh, &sh_found);
+  ls_fallback_block(a, scen, a.state[scen], sh, &sh_found);
 }
 
 // Where iteration `it` of a scenario writes its adjoint tape: every
@@ -2519,7 +2492,7 @@ cudaError_t launch_ls_pass(const LinkArgs& a, int grid, int block, cudaStream_t 
 }
 
 cudaError_t launch_ls_fallback(const LinkArgs& a, cudaStream_t s) {
-  k_ls_fallback<<<dim3(1, a.num_scen), kLsRestBlock, 0, s>>>(a);
+  k_ls_fallback<<<dim3(1, a.num_scen), 1024, 0, s>>>(a);
   return cudaGetLastError();
 }
 

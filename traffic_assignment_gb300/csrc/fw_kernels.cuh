@@ -200,7 +200,6 @@ cudaError_t launch_set_costs(const LinkArgs& a, int grid, cudaStream_t s);
 // most kSmallNet links, FP64 work over more SMs) or kLinkBlock
 constexpr int kSmallLinkBlock = 64;
 cudaError_t launch_ls_pass(const LinkArgs& a, int grid, int block, cudaStream_t s);
-// the line-search passes from a.pass on and the fallback, one block per scenario
 cudaError_t launch_ls_fallback(const LinkArgs& a, cudaStream_t s);
 cudaError_t launch_step(const LinkArgs& a, int grid, int block, cudaStream_t s);
 // small networks (at most kSmallTail links): every line-search pass, the

@@ -463,22 +463,17 @@ int Ctx::enqueue_iteration(int nscen) {
     return TAPGPU_OK;
   }
   TG_TRY(mark(2, true));
-  // the 2^-k rule on small networks: the first pass over all SMs, the rest
-  // (rarely any work) in the fallback's launch; otherwise every pass over all
-  // SMs, the fallback after them
   const int passes = ls_mode == kLsExact ? kLsExactPasses : kLsPasses;
-  const int multi = ls_mode != kLsExact && M <= kSmallNet ? 1 : passes;
-  for (int p = 0; p < multi; ++p) {
+  for (int p = 0; p < passes; ++p) {
     la.pass = p;
     TG_CUDA(launch_ls_pass(la, ls_grid(nscen), ls_block, stream));
   }
-  la.pass = multi;
   TG_CUDA(launch_ls_fallback(la, stream));
   TG_TRY(mark(2, false));
   TG_TRY(mark(3, true));
   TG_CUDA(launch_step(la, ls_link_grid, ls_block, stream));
   TG_TRY(mark(3, false));
-  count_launches(multi + 2);
+  count_launches(passes + 2);
   return TAPGPU_OK;
 }
 
@@ -1767,13 +1762,10 @@ int tapgpu_profile_iteration(tapgpu_ctx* ctx, int reps, float* ms) {
                        c->aon_smem, c->stream);
     cudaEventRecord(ev[2], c->stream);
     tapgpu::LinkArgs la = c->link_args(1);
-    const int passes = c->ls_mode == tapgpu::kLsExact ? tapgpu::kLsExactPasses : tapgpu::kLsPasses;
-    const int multi = c->ls_mode != tapgpu::kLsExact && c->M <= tapgpu::kSmallNet ? 1 : passes;
-    for (int p = 0; p < multi; ++p) {
+    for (int p = 0; p < tapgpu::kLsPasses; ++p) {
       la.pass = p;
       tapgpu::launch_ls_pass(la, c->ls_grid(1), c->ls_block, c->stream);
     }
-    la.pass = multi;
     tapgpu::launch_ls_fallback(la, c->stream);
     cudaEventRecord(ev[3], c->stream);
     tapgpu::launch_step(la, c->ls_link_grid, c->ls_block, c->stream);
