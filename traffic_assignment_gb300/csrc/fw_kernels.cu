@@ -1325,7 +1325,8 @@ __device__ __forceinline__ int parent_of(const int* parent, const unsigned short
 // later the 64-bit totals, and the predecessor words go to the task's slot of
 // the label buffer, free once its labels are in shared memory (its second
 // half serves as scratch); parents are 16-bit.  Otherwise 16 bytes per node:
-// totals (labels first), predecessor links, parents.
+// totals (labels first), predecessor links, parents (12 bytes with FP32
+// labels, whose totals are 32-bit).
 template <typename T, int BLOCK, bool SMEM, bool COMPACT>
 __global__ void __launch_bounds__(BLOCK, COMPACT ? (sizeof(T) == 4 ? 2048 : 1024) / BLOCK : 1)
     k_aon(PathArgs a) {
@@ -1339,9 +1340,10 @@ __global__ void __launch_bounds__(BLOCK, COMPACT ? (sizeof(T) == 4 ? 2048 : 1024
            : static_cast<unsigned char*>(a.scratch) + static_cast<size_t>(blockIdx.x) * a.scratch_stride;
   T* dS = reinterpret_cast<T*>(base);                         // labels, then ...
   long long* thr = reinterpret_cast<long long*>(base);        // ... node throughput
-  int* pred = COMPACT ? reinterpret_cast<int*>(base + 4 * static_cast<size_t>(n1))
-                      : reinterpret_cast<int*>(base + align16(sizeof(long long) * n1));
-  int* parent = pred + n1;  // (16-byte layout)
+  int* pred = COMPACT
+                  ? reinterpret_cast<int*>(base + 4 * static_cast<size_t>(n1))
+                  : reinterpret_cast<int*>(base + align16(sizeof(T) * static_cast<size_t>(n1)));
+  int* parent = pred + n1;  // (16- or 12-byte layout)
   unsigned short* par16 = reinterpret_cast<unsigned short*>(base + align16(8 * static_cast<size_t>(n1)));
   const int F = a.g.first_thru;
 
@@ -2354,7 +2356,7 @@ bool aon_compact(int n1, bool fp64) { return !fp64 && n1 <= 0xffff; }
 size_t aon_smem_bytes(int n1, bool fp64, bool c64) {
   const size_t n = static_cast<size_t>(n1);
   if (aon_compact(n1, fp64) || (fp64 && c64)) return align16(align16(8 * n) + align16(2 * n));
-  return align16(align16(8 * n) + 2 * 4 * n);
+  return align16(align16((fp64 ? 8 : 4) * n) + 2 * 4 * n);  // (FP32: 4-byte labels and totals)
 }
 
 int max_smem_optin(int device) {
